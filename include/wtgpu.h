@@ -1,0 +1,181 @@
+/*
+ * wtgpu.h — C ABI of the GB300-native surface Green's-function path for
+ * WannierTools (quanshengwu/wannier_tools 2.7.1).
+ *
+ * The library replaces, behind plain C entry points, the per-(k, omega) hot
+ * path of the reference's surface-state drivers:
+ *
+ *   ham_qlayer2qlayer(k, H00, H01)                src/ham_qlayer2qlayer.f90:1-102
+ *   surfgreen_1985(omega, GLL, GRR, GB, H00, H01, ones, eta)
+ *                                                  src/surfgreen.f90:7-137
+ *   inv / mat_mul (zgesv / zgemm)                  src/inverse.f90:1-58, src/mat_mul.f90:3-27
+ *   the k x omega loop bodies of surfstat          src/surfstat.f90:123-197
+ *   and of SurfaceDOSkk                            src/fermiarc.f90:206-248
+ *
+ * Conventions (those of the reference, so a Fortran iso_c_binding interface
+ * can pass its arrays unchanged):
+ *   - complex arrays are interleaved (re, im) double pairs, i.e. the memory
+ *     layout of Fortran complex(dp) / C99 double _Complex;
+ *   - matrices are column-major, leading dimension = their row count;
+ *   - orbital index lists (top / bottom) are 1-based, as TopOrbitals /
+ *     BottomOrbitals in src/module.f90;
+ *   - energies are in Hartree (src/readinput.f90:721-724);
+ *   - the caller owns every buffer it passes; the library copies in and out.
+ *
+ * Return codes: WTG_OK (0) on success; > 0 when at least one (k, omega)
+ * point carries a warning bit in its status entry (count of such points,
+ * saturated at INT32_MAX); < 0 on hard errors.  The library never calls
+ * exit/abort.  A textual reason for the last error of the calling thread is
+ * available from wtg_last_error.
+ *
+ * Threading: distinct model handles are independent.  Calls on one handle
+ * are serialised by the library (host side) and ordered on the GPU.
+ */
+#ifndef WTGPU_H
+#define WTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* hard error codes */
+#define WTG_OK              0
+#define WTG_EINVAL         -1   /* bad argument */
+#define WTG_ENOMEM         -2   /* device or host allocation failed */
+#define WTG_ECUDA          -3   /* CUDA runtime error */
+#define WTG_ENODEV         -4   /* no usable CUDA device */
+#define WTG_EUNSUPPORTED   -6   /* size / mode not supported by this build */
+
+/* per-point status bits (status[] outputs) */
+#define WTG_PT_NOT_CONVERGED 1  /* itermax reached, sum|alpha| > tol (src/surfgreen.f90:86-123) */
+#define WTG_PT_SINGULAR      2  /* exact zero pivot; the inverse is replaced by the
+                                   identity, as zgesv+inv do (src/inverse.f90:51-55) */
+#define WTG_PT_NONFINITE     4  /* a spectral sum is NaN or Inf */
+
+/* precision modes */
+#define WTG_PREC_FP64  0        /* all-FP64 decimation */
+
+typedef struct wtg_model* wtg_model_t;
+
+/*
+ * Upload a principal-layer tight-binding model and keep it resident on the
+ * device.  Replaces the module-global state read by ham_qlayer2qlayer
+ * (HmnR_surfacecell / irvec_surfacecell / ndegen_surfacecell produced by
+ * get_hmnr_cell, src/readHmnR.f90:578-766; Np and ijmax, src/module.f90:503-507).
+ *
+ *   nw      Num_wann
+ *   nrpts   nrpts_surfacecell
+ *   irvec   int[3*nrpts], column-major (3, nrpts) like irvec_surfacecell
+ *   hmnr    complex[nw*nw*nrpts], column-major (nw, nw, nrpts), Hartree
+ *   ndegen  int[nrpts] (NULL = all ones); each term is divided by it as at
+ *           src/ham_qlayer2qlayer.f90:60
+ *   np      number of principal layers Np (Ndim = nw*np)
+ *   ijmax   layer cut-off (reference default 10, src/module.f90:505)
+ */
+int wtg_model_create(int nw, int nrpts, const int* irvec, const double* hmnr,
+                     const int* ndegen, int np, int ijmax, wtg_model_t* out);
+
+/* Release a model and all device memory it holds. */
+int wtg_model_destroy(wtg_model_t model);
+
+/* Ndim = nw*np of a model (or < 0 on a bad handle). */
+int wtg_model_ndim(wtg_model_t model);
+
+/*
+ * H00/H01 for one in-plane k (fractional surface-BZ coordinates, k[2]).
+ * Replaces ham_qlayer2qlayer(k, H00, H01), src/ham_qlayer2qlayer.f90:1-102.
+ * h00, h01: complex[Ndim*Ndim] column-major (host buffers).
+ */
+int wtg_ham_qlayer2qlayer(wtg_model_t model, const double* k, double* h00, double* h01);
+
+/*
+ * One Lopez-Sancho decimation on the GPU with full outputs.
+ * Replaces surfgreen_1985(omega, GLL, GRR, GB, H00, H01, ones, eta),
+ * src/surfgreen.f90:7-137 (the identity "ones" argument is implicit).
+ *   tol      convergence threshold on sum_ij |alpha_ij| (reference: 1e-16
+ *            single-precision literal, src/surfgreen.f90:42)
+ *   itermax  iteration cap (reference: 100, src/surfgreen.f90:39)
+ * h00/h01 in, gll/grr/gb out: complex[ndim*ndim] column-major host buffers.
+ * iters / status (may be NULL): iterations executed and WTG_PT_* bits.
+ */
+int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00,
+                       const double* h01, double tol, int itermax,
+                       double* gll, double* grr, double* gb,
+                       int* iters, int* status);
+
+/*
+ * Batched surface spectrum over an explicit k list x omega list: for every
+ * (k, omega) the Fourier sum of ham_qlayer2qlayer, one surfgreen_1985
+ * decimation, and the spectral sums
+ *   dos_l(ik,j)    = - sum_{io in top}  Im GLL(io,io)            * scale
+ *   dos_r(ik,j)    = - sum_{io in bot}  Im GRR(Ndim-nw+io, same) * scale
+ *   dos_bulk(ik,j) = - sum_{i=1..Ndim}  Im GB(i,i)               * scale
+ * i.e. the loop bodies of surfstat (scale = 1, src/surfstat.f90:123-160)
+ * and SurfaceDOSkk (scale = 1/pi applied per term, src/fermiarc.f90:206-248).
+ *
+ *   k        double[nk*2], column-major (nk, 2) like k2_path (src/module.f90)
+ *   omega    double[nomega], Hartree
+ *   eta      broadening, Hartree (surfstat: 3*(wmax-wmin)/nomega,
+ *            src/surfstat.f90:84; SurfaceDOSkk: Fermi_broadening,
+ *            src/fermiarc.f90:194)
+ *   top/bot  1-based orbital lists (TopOrbitals / BottomOrbitals)
+ *   divide_by_pi  0 for surfstat, 1 for SurfaceDOSkk
+ *   precision     WTG_PREC_FP64
+ *   dos_l, dos_r, dos_bulk  double[nk*nomega], column-major (nk, nomega)
+ *   iters (int32) / status (uint8) [nk*nomega], optional (NULL)
+ * All pointers are host pointers.
+ */
+int wtg_surface_spectrum(wtg_model_t model, int nk, const double* k,
+                         int nomega, const double* omega, double eta,
+                         double tol, int itermax,
+                         int ntop, const int* top, int nbot, const int* bot,
+                         int divide_by_pi, int precision,
+                         double* dos_l, double* dos_r, double* dos_bulk,
+                         int32_t* iters, uint8_t* status);
+
+/*
+ * Same computation with every array already on the device, enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) without a host
+ * synchronisation.  top/bot are host arrays (they are small and copied
+ * into the launch).  Returns after enqueueing; per-point status is in
+ * `status` once the stream reaches that point.
+ */
+int wtg_surface_spectrum_device(wtg_model_t model, int nk, const double* d_k,
+                                int nomega, const double* d_omega, double eta,
+                                double tol, int itermax,
+                                int ntop, const int* top, int nbot, const int* bot,
+                                int divide_by_pi, int precision,
+                                double* d_dos_l, double* d_dos_r, double* d_dos_bulk,
+                                int32_t* d_iters, uint8_t* d_status, void* stream);
+
+/*
+ * Tracing (no reference counterpart beyond its wall-clock timers,
+ * src/wt_aux.f90:6-37 and the time_q / time_ss split of
+ * src/fermiarc.f90:214-232).  wtg_model_profile(m, 1) resets the counters
+ * and records CUDA events around every Fourier-sum and decimation launch of
+ * the handle; wtg_model_profile_read synchronises them and returns the
+ * summed device milliseconds of each phase, the number of this library's
+ * kernels the handle has launched since the reset, and the number of
+ * decimation launches.
+ */
+int wtg_model_profile(wtg_model_t model, int enable);
+int wtg_model_profile_read(wtg_model_t model, double* fourier_ms, double* decim_ms,
+                           long long* launches, int* decim_launches);
+
+/* FP64 (DFMA) throughput of the current device in TFLOP/s: the roofline
+   denominator of the FP64 path, measured with a short throughput kernel. */
+int wtg_probe_fp64_peak(double* tflops);
+
+/* Copy the calling thread's last error message into buf (NUL-terminated). */
+int wtg_last_error(char* buf, int len);
+
+/* Describe the device the library runs on ("name, SMs, cc") into buf. */
+int wtg_device_info(char* buf, int len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WTGPU_H */

@@ -1,0 +1,541 @@
+// C ABI of the surface Green's-function path (declarations: include/wtgpu.h).
+//
+// Host side: validation, model upload (HmnR resident in HBM, grouped by R3),
+// device buffers, k chunking, launch configuration, host<->device staging for
+// the host-pointer entry points.  No CPU computation of the path happens here:
+// every H00/H01, inverse, product and spectral sum is computed by the kernels
+// in wtg_fourier.cu / wtg_decimate.cu.
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/wtgpu.h"
+#include "wtg_common.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return WTG_ECUDA;
+}
+
+#define WTG_CK(call)                                  \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// grow-only device buffer
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Upper bound on the H00/H01 buffer of one k chunk.
+constexpr size_t H_CHUNK_BYTES = (size_t)8 << 30;
+
+}  // namespace
+
+struct wtg_model {
+  int device = 0;
+  int nw = 0, nR = 0, np = 0, ijmax = 0, N = 0;
+  int ic_lo = 0, nic = 0, nRu = 0;
+  double2* d_hr = nullptr;
+  double2* d_rab = nullptr;
+  int* d_icoff = nullptr;
+  DevBuf phase, h, ws, counter;
+  // staging for the host-pointer entry points
+  DevBuf k_in, w_in, out_dos, out_it, out_st;
+  cudaStream_t stream = nullptr;       // stream of the host-pointer entry points
+  cudaEvent_t done = nullptr;          // orders calls on this handle on the GPU
+  std::mutex mu;
+  // tracing: CUDA events around each Fourier / decimation launch
+  bool profile = false;
+  long long launches = 0;              // kernels of this library launched by the handle
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<size_t, size_t>> fourier_ev, decim_ev;
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e = nullptr;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+};
+
+namespace {
+
+int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const double* d_omega,
+                 double eta, double tol, int itermax, int ntop, const int* top, int nbot,
+                 const int* bot, int divide_by_pi, double* d_dl, double* d_dr, double* d_db,
+                 int32_t* d_it, uint8_t* d_st, cudaStream_t s) {
+  const int N = m->N;
+  if (N > wtg::decim_fp64_max_n())
+    return fail(WTG_EUNSUPPORTED, "Ndim " + std::to_string(N) + " exceeds the FP64 kernel limit " +
+                                      std::to_string(wtg::decim_fp64_max_n()));
+  wtg::DecimConfig cfg;
+  int thr = 0;
+  if (const char* env = getenv("WTG_DECIM_THREADS")) thr = atoi(env);
+  WTG_CK(wtg::decim_fp64_config(N, thr, &cfg));
+  if (cfg.ctas_per_sm < 1) return fail(WTG_EUNSUPPORTED, "decimation kernel does not fit an SM");
+  int nsm = 0;
+  WTG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, m->device));
+
+  const size_t hk = sizeof(double2) * 2 * (size_t)N * N;   // H00+H01 per k
+  int kchunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nk, H_CHUNK_BYTES / hk));
+  kchunk = std::min(kchunk, 65535 * 8);
+  const long long max_inst = (long long)kchunk * nomega;
+  const int grid_max = cfg.ctas_per_sm * nsm;
+  const int grid = (int)std::min<long long>(grid_max, max_inst);
+
+  WTG_CK(m->phase.ensure(sizeof(double2) * (size_t)kchunk * std::max(1, m->nRu)));
+  WTG_CK(m->h.ensure(hk * kchunk));
+  WTG_CK(m->ws.ensure(sizeof(double2) * 8 * (size_t)N * N * grid));
+  WTG_CK(m->counter.ensure(sizeof(int) * 64));
+
+  WTG_CK(cudaStreamWaitEvent(s, m->done, 0));
+  wtg::DecimArgs a;
+  memset(&a, 0, sizeof(a));
+  a.N = N;
+  a.nw = m->nw;
+  a.nomega = nomega;
+  a.omega = d_omega;
+  a.eta = eta;
+  a.tol = tol;
+  a.itermax = itermax;
+  a.divide_by_pi = divide_by_pi;
+  a.nk_total = nk;
+  a.dos_l = d_dl;
+  a.dos_r = d_dr;
+  a.dos_bulk = d_db;
+  a.iters = d_it;
+  a.status = d_st;
+  a.ws = (double2*)m->ws.p;
+  a.KC = cfg.KC;
+  a.ntop = ntop;
+  a.nbot = nbot;
+  for (int q = 0; q < ntop; ++q) a.top[q] = top[q];
+  for (int q = 0; q < nbot; ++q) a.bot[q] = bot[q];
+  int chunk_id = 0;
+  for (int k0 = 0; k0 < nk; k0 += kchunk, ++chunk_id) {
+    const int kc = std::min(kchunk, nk - k0);
+    wtg::FourierArgs f;
+    f.k = d_k;
+    f.nk_total = nk;
+    f.k0 = k0;
+    f.kc = kc;
+    f.rab = m->d_rab;
+    f.hr = m->d_hr;
+    f.icoff = m->d_icoff;
+    f.ic_lo = m->ic_lo;
+    f.nic = m->nic;
+    f.nRu = m->nRu;
+    f.nw = m->nw;
+    f.np = m->np;
+    f.ijmax = m->ijmax;
+    f.phase = (double2*)m->phase.p;
+    f.h = (double2*)m->h.p;
+    const size_t fe0 = m->ev_used;
+    if (m->profile) WTG_CK(cudaEventRecord(m->next_event(), s));
+    wtg::launch_fourier(f, s);
+    WTG_CK(cudaGetLastError());
+    m->launches += (kc > 0 && m->nRu > 0 ? 1 : 0) + (m->nic > 0 ? 1 : 0);
+    if (m->profile) {
+      WTG_CK(cudaEventRecord(m->next_event(), s));
+      m->fourier_ev.push_back({fe0, fe0 + 1});
+    }
+    int* ctr = (int*)m->counter.p + (chunk_id & 63);
+    WTG_CK(cudaMemsetAsync(ctr, 0, sizeof(int), s));
+    a.h = (const double2*)m->h.p;
+    a.n_inst = kc * nomega;
+    a.k_offset = k0;
+    a.counter = ctr;
+    const int g = (int)std::min<long long>(grid, a.n_inst);
+    const size_t de0 = m->ev_used;
+    if (m->profile) WTG_CK(cudaEventRecord(m->next_event(), s));
+    WTG_CK(wtg::launch_decimate_fp64(a, cfg, g, s));
+    m->launches += 1;
+    if (m->profile) {
+      WTG_CK(cudaEventRecord(m->next_event(), s));
+      m->decim_ev.push_back({de0, de0 + 1});
+    }
+  }
+  WTG_CK(cudaEventRecord(m->done, s));
+  return WTG_OK;
+}
+
+int check_lists(int nw, int ntop, const int* top, int nbot, const int* bot) {
+  if (ntop < 0 || nbot < 0 || ntop > wtg::MAX_ORB || nbot > wtg::MAX_ORB)
+    return fail(WTG_EINVAL, "orbital list length out of range [0, 1024]");
+  if ((ntop > 0 && !top) || (nbot > 0 && !bot)) return fail(WTG_EINVAL, "null orbital list");
+  for (int q = 0; q < ntop; ++q)
+    if (top[q] < 1 || top[q] > nw) return fail(WTG_EINVAL, "top orbital index outside 1..nw");
+  for (int q = 0; q < nbot; ++q)
+    if (bot[q] < 1 || bot[q] > nw) return fail(WTG_EINVAL, "bottom orbital index outside 1..nw");
+  return WTG_OK;
+}
+
+int count_flagged(const uint8_t* st, size_t n) {
+  long long c = 0;
+  for (size_t i = 0; i < n; ++i) c += st[i] != 0;
+  return (int)std::min<long long>(c, INT_MAX);
+}
+
+}  // namespace
+
+extern "C" {
+
+int wtg_model_create(int nw, int nrpts, const int* irvec, const double* hmnr, const int* ndegen,
+                     int np, int ijmax, wtg_model_t* out) {
+  if (!out) return fail(WTG_EINVAL, "out is null");
+  *out = nullptr;
+  if (nw < 1 || nrpts < 0 || np < 1 || ijmax < 0)
+    return fail(WTG_EINVAL, "nw, np must be >= 1; nrpts, ijmax >= 0");
+  if (nrpts > 0 && (!irvec || !hmnr)) return fail(WTG_EINVAL, "irvec/hmnr null");
+  if ((long long)nw * np > 4096) return fail(WTG_EINVAL, "Ndim too large");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(WTG_ENODEV, "no CUDA device available");
+  wtg_model* m = new wtg_model();
+  cudaGetDevice(&m->device);
+  m->nw = nw;
+  m->nR = nrpts;
+  m->np = np;
+  m->ijmax = ijmax;
+  m->N = nw * np;
+  // R3 values that reach H00 (|j-i| <= Np-1) or H01 (1 <= j-i <= 2Np-1),
+  // cut at |R3| <= ijmax (src/ham_qlayer2qlayer.f90:54,72,83).
+  const int lo = std::max(-(np - 1), -ijmax), hi = std::min(2 * np - 1, ijmax);
+  m->ic_lo = lo;
+  m->nic = hi >= lo ? hi - lo + 1 : 0;
+  std::vector<int> order;
+  for (int r = 0; r < nrpts; ++r) {
+    const int ic = irvec[3 * r + 2];
+    if (ic >= lo && ic <= hi) order.push_back(r);
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return irvec[3 * x + 2] < irvec[3 * y + 2]; });
+  m->nRu = (int)order.size();
+  std::vector<int> icoff(m->nic + 1, 0);
+  for (int r : order) icoff[irvec[3 * r + 2] - lo + 1]++;
+  for (int g = 0; g < m->nic; ++g) icoff[g + 1] += icoff[g];
+  const size_t nw2 = (size_t)nw * nw;
+  std::vector<double2> hr(std::max<size_t>(1, nw2 * m->nRu));
+  std::vector<double2> rab(std::max(1, m->nRu));
+  for (int u = 0; u < m->nRu; ++u) {
+    const int r = order[u];
+    const double nd = ndegen ? (double)ndegen[r] : 1.0;
+    if (nd == 0.0) {
+      delete m;
+      return fail(WTG_EINVAL, "ndegen entry is zero");
+    }
+    for (size_t e = 0; e < nw2; ++e) {
+      const double re = hmnr[2 * (nw2 * r + e)], im = hmnr[2 * (nw2 * r + e) + 1];
+      hr[nw2 * u + e] = make_double2(nd == 1.0 ? re : re / nd, nd == 1.0 ? im : im / nd);
+    }
+    rab[u] = make_double2((double)irvec[3 * r], (double)irvec[3 * r + 1]);
+  }
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_hr, sizeof(double2) * hr.size());
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_rab, sizeof(double2) * rab.size());
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_icoff, sizeof(int) * icoff.size());
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_hr, hr.data(), sizeof(double2) * hr.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_rab, rab.data(), sizeof(double2) * rab.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_icoff, icoff.data(), sizeof(int) * icoff.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(m->done, m->stream);
+  if (e != cudaSuccess) {
+    wtg_model_destroy(m);
+    return cuda_fail(e, "wtg_model_create");
+  }
+  *out = m;
+  return WTG_OK;
+}
+
+int wtg_model_destroy(wtg_model_t m) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  {
+    std::lock_guard<std::mutex> lk(m->mu);
+    cudaSetDevice(m->device);
+    if (m->done) cudaEventSynchronize(m->done);
+    cudaFree(m->d_hr);
+    cudaFree(m->d_rab);
+    cudaFree(m->d_icoff);
+    m->phase.release();
+    m->h.release();
+    m->ws.release();
+    m->counter.release();
+    m->k_in.release();
+    m->w_in.release();
+    m->out_dos.release();
+    m->out_it.release();
+    m->out_st.release();
+    if (m->done) cudaEventDestroy(m->done);
+    for (cudaEvent_t e : m->ev_pool) cudaEventDestroy(e);
+    if (m->stream) cudaStreamDestroy(m->stream);
+  }
+  delete m;
+  return WTG_OK;
+}
+
+int wtg_model_ndim(wtg_model_t m) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  return m->N;
+}
+
+int wtg_ham_qlayer2qlayer(wtg_model_t m, const double* k, double* h00, double* h01) {
+  if (!m || !k || !h00 || !h01) return fail(WTG_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(m->mu);
+  WTG_CK(cudaSetDevice(m->device));
+  cudaStream_t s = m->stream;
+  WTG_CK(cudaStreamWaitEvent(s, m->done, 0));
+  WTG_CK(m->k_in.ensure(sizeof(double) * 2));
+  WTG_CK(m->phase.ensure(sizeof(double2) * std::max(1, m->nRu)));
+  const size_t nn = (size_t)m->N * m->N;
+  WTG_CK(m->h.ensure(sizeof(double2) * 2 * nn));
+  WTG_CK(cudaMemcpyAsync(m->k_in.p, k, sizeof(double) * 2, cudaMemcpyHostToDevice, s));
+  wtg::FourierArgs f;
+  f.k = (const double*)m->k_in.p;
+  f.nk_total = 1;
+  f.k0 = 0;
+  f.kc = 1;
+  f.rab = m->d_rab;
+  f.hr = m->d_hr;
+  f.icoff = m->d_icoff;
+  f.ic_lo = m->ic_lo;
+  f.nic = m->nic;
+  f.nRu = m->nRu;
+  f.nw = m->nw;
+  f.np = m->np;
+  f.ijmax = m->ijmax;
+  f.phase = (double2*)m->phase.p;
+  f.h = (double2*)m->h.p;
+  wtg::launch_fourier(f, s);
+  WTG_CK(cudaGetLastError());
+  WTG_CK(cudaMemcpyAsync(h00, f.h, sizeof(double2) * nn, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(h01, f.h + nn, sizeof(double2) * nn, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaEventRecord(m->done, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  return WTG_OK;
+}
+
+int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00, const double* h01,
+                       double tol, int itermax, double* gll, double* grr, double* gb, int* iters,
+                       int* status) {
+  if (ndim < 1 || !h00 || !h01 || !gll || !grr || !gb) return fail(WTG_EINVAL, "bad argument");
+  if (itermax < 0) return fail(WTG_EINVAL, "itermax < 0");
+  if (ndim > wtg::decim_fp64_max_n())
+    return fail(WTG_EUNSUPPORTED, "Ndim exceeds the FP64 kernel limit");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(WTG_ENODEV, "no CUDA device available");
+  const size_t nn = (size_t)ndim * ndim;
+  wtg::DecimConfig cfg;
+  WTG_CK(wtg::decim_fp64_config(ndim, 0, &cfg));
+  // one allocation: h[2nn] | gll gll grr gb [3nn] | ws [8nn] | omega | outputs
+  const size_t bytes = sizeof(double2) * (13 * nn) + 64 + 64;
+  char* base = nullptr;
+  WTG_CK(cudaMalloc(&base, bytes));
+  double2* dh = (double2*)base;
+  double2* dgll = dh + 2 * nn;
+  double2* dgrr = dgll + nn;
+  double2* dgb = dgrr + nn;
+  double2* dws = dgb + nn;
+  char* tail = (char*)(dws + 8 * nn);
+  double* dw = (double*)tail;          // omega
+  double* ddos = dw + 1;               // 3 doubles
+  int* dctr = (int*)(ddos + 3);
+  int32_t* dit = dctr + 1;
+  uint8_t* dst = (uint8_t*)(dit + 1);
+  int rc = WTG_OK;
+  cudaError_t e = cudaMemcpy(dh, h00, sizeof(double2) * nn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dh + nn, h01, sizeof(double2) * nn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dw, &omega, sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dctr, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    wtg::DecimArgs a;
+    memset(&a, 0, sizeof(a));
+    a.N = ndim;
+    a.nw = ndim;
+    a.nomega = 1;
+    a.n_inst = 1;
+    a.h = dh;
+    a.omega = dw;
+    a.eta = eta;
+    a.tol = tol;
+    a.itermax = itermax;
+    a.nk_total = 1;
+    a.dos_l = ddos;
+    a.dos_r = ddos + 1;
+    a.dos_bulk = ddos + 2;
+    a.iters = dit;
+    a.status = dst;
+    a.gll = dgll;
+    a.grr = dgrr;
+    a.gb = dgb;
+    a.ws = dws;
+    a.counter = dctr;
+    a.KC = cfg.KC;
+    e = wtg::launch_decimate_fp64(a, cfg, 1, 0);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(gll, dgll, sizeof(double2) * nn, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(grr, dgrr, sizeof(double2) * nn, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(gb, dgb, sizeof(double2) * nn, cudaMemcpyDeviceToHost);
+  int32_t it = 0;
+  uint8_t st = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&it, dit, sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&st, dst, sizeof(uint8_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) rc = cuda_fail(e, "wtg_surfgreen_1985");
+  cudaFree(base);
+  if (rc != WTG_OK) return rc;
+  if (iters) *iters = it;
+  if (status) *status = st;
+  return st ? 1 : WTG_OK;
+}
+
+int wtg_surface_spectrum_device(wtg_model_t m, int nk, const double* d_k, int nomega,
+                                const double* d_omega, double eta, double tol, int itermax,
+                                int ntop, const int* top, int nbot, const int* bot,
+                                int divide_by_pi, int precision, double* d_dos_l, double* d_dos_r,
+                                double* d_dos_bulk, int32_t* d_iters, uint8_t* d_status,
+                                void* stream) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  if (nk < 0 || nomega < 0 || itermax < 0) return fail(WTG_EINVAL, "negative size");
+  if (precision != WTG_PREC_FP64) return fail(WTG_EUNSUPPORTED, "precision mode not built");
+  if (nk == 0 || nomega == 0) return WTG_OK;
+  if (!d_k || !d_omega || !d_dos_l || !d_dos_r || !d_dos_bulk) return fail(WTG_EINVAL, "null array");
+  int rc = check_lists(m->nw, ntop, top, nbot, bot);
+  if (rc != WTG_OK) return rc;
+  std::lock_guard<std::mutex> lk(m->mu);
+  WTG_CK(cudaSetDevice(m->device));
+  return run_spectrum(m, nk, d_k, nomega, d_omega, eta, tol, itermax, ntop, top, nbot, bot,
+                      divide_by_pi, d_dos_l, d_dos_r, d_dos_bulk, d_iters, d_status,
+                      (cudaStream_t)stream);
+}
+
+int wtg_surface_spectrum(wtg_model_t m, int nk, const double* k, int nomega, const double* omega,
+                         double eta, double tol, int itermax, int ntop, const int* top, int nbot,
+                         const int* bot, int divide_by_pi, int precision, double* dos_l,
+                         double* dos_r, double* dos_bulk, int32_t* iters, uint8_t* status) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  if (nk < 0 || nomega < 0 || itermax < 0) return fail(WTG_EINVAL, "negative size");
+  if (precision != WTG_PREC_FP64) return fail(WTG_EUNSUPPORTED, "precision mode not built");
+  if (nk == 0 || nomega == 0) return WTG_OK;
+  if (!k || !omega || !dos_l || !dos_r || !dos_bulk) return fail(WTG_EINVAL, "null array");
+  int rc = check_lists(m->nw, ntop, top, nbot, bot);
+  if (rc != WTG_OK) return rc;
+  std::lock_guard<std::mutex> lk(m->mu);
+  WTG_CK(cudaSetDevice(m->device));
+  const size_t npts = (size_t)nk * nomega;
+  cudaStream_t s = m->stream;
+  WTG_CK(cudaStreamWaitEvent(s, m->done, 0));
+  WTG_CK(m->k_in.ensure(sizeof(double) * 2 * (size_t)nk));
+  WTG_CK(m->w_in.ensure(sizeof(double) * (size_t)nomega));
+  WTG_CK(m->out_dos.ensure(sizeof(double) * 3 * npts));
+  WTG_CK(m->out_it.ensure(sizeof(int32_t) * npts));
+  WTG_CK(m->out_st.ensure(sizeof(uint8_t) * npts));
+  WTG_CK(cudaMemcpyAsync(m->k_in.p, k, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice, s));
+  WTG_CK(cudaMemcpyAsync(m->w_in.p, omega, sizeof(double) * nomega, cudaMemcpyHostToDevice, s));
+  double* dd = (double*)m->out_dos.p;
+  rc = run_spectrum(m, nk, (const double*)m->k_in.p, nomega, (const double*)m->w_in.p, eta, tol,
+                    itermax, ntop, top, nbot, bot, divide_by_pi, dd, dd + npts, dd + 2 * npts,
+                    (int32_t*)m->out_it.p, (uint8_t*)m->out_st.p, s);
+  if (rc != WTG_OK) return rc;
+  WTG_CK(cudaMemcpyAsync(dos_l, dd, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(dos_r, dd + npts, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(dos_bulk, dd + 2 * npts, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
+  std::vector<uint8_t> st_local;
+  uint8_t* st_host = status;
+  if (!st_host) {
+    st_local.resize(npts);
+    st_host = st_local.data();
+  }
+  WTG_CK(cudaMemcpyAsync(st_host, m->out_st.p, npts, cudaMemcpyDeviceToHost, s));
+  if (iters)
+    WTG_CK(cudaMemcpyAsync(iters, m->out_it.p, sizeof(int32_t) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  return count_flagged(st_host, npts);
+}
+
+int wtg_model_profile(wtg_model_t m, int enable) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  std::lock_guard<std::mutex> lk(m->mu);
+  if (m->done) cudaEventSynchronize(m->done);
+  m->profile = enable != 0;
+  m->ev_used = 0;
+  m->fourier_ev.clear();
+  m->decim_ev.clear();
+  m->launches = 0;
+  return WTG_OK;
+}
+
+int wtg_model_profile_read(wtg_model_t m, double* fourier_ms, double* decim_ms,
+                           long long* launches, int* decim_launches) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  std::lock_guard<std::mutex> lk(m->mu);
+  WTG_CK(cudaSetDevice(m->device));
+  WTG_CK(cudaEventSynchronize(m->done));
+  double tf = 0.0, td = 0.0;
+  for (auto& pr : m->fourier_ev) {
+    float ms = 0.f;
+    WTG_CK(cudaEventElapsedTime(&ms, m->ev_pool[pr.first], m->ev_pool[pr.second]));
+    tf += ms;
+  }
+  for (auto& pr : m->decim_ev) {
+    float ms = 0.f;
+    WTG_CK(cudaEventElapsedTime(&ms, m->ev_pool[pr.first], m->ev_pool[pr.second]));
+    td += ms;
+  }
+  if (fourier_ms) *fourier_ms = tf;
+  if (decim_ms) *decim_ms = td;
+  if (launches) *launches = m->launches;
+  if (decim_launches) *decim_launches = (int)m->decim_ev.size();
+  return WTG_OK;
+}
+
+int wtg_last_error(char* buf, int len) {
+  if (!buf || len <= 0) return WTG_EINVAL;
+  snprintf(buf, (size_t)len, "%s", g_err.c_str());
+  return WTG_OK;
+}
+
+int wtg_device_info(char* buf, int len) {
+  if (!buf || len <= 0) return WTG_EINVAL;
+  int dev = 0;
+  cudaDeviceProp p;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess)
+    return fail(WTG_ENODEV, "no CUDA device available");
+  snprintf(buf, (size_t)len, "%s, %d SMs, cc %d.%d, %.1f GiB", p.name, p.multiProcessorCount,
+           p.major, p.minor, p.totalGlobalMem / 1073741824.0);
+  return WTG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// Shared declarations of the GB300 (sm_103a) surface Green's-function kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace wtg {
+
+// The reference's truncated pi literal (src/module.f90:719); the Fourier
+// phases use it exactly as ham_qlayer2qlayer does (src/ham_qlayer2qlayer.f90:56).
+constexpr double PI_REF = 3.14159265358979;
+
+constexpr int MAX_ORB = 1024;     // longest top / bottom orbital list per launch
+
+// per-point status bits (mirrors WTG_PT_* of include/wtgpu.h)
+constexpr int PT_NOT_CONVERGED = 1;
+constexpr int PT_SINGULAR = 2;
+constexpr int PT_NONFINITE = 4;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+// acc += a*b with four fused multiply-adds (one complex multiply-accumulate)
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+
+// ---------------------------------------------------------------------------
+// Principal-layer Fourier sum (ham_qlayer2qlayer)
+// ---------------------------------------------------------------------------
+struct FourierArgs {
+  const double* k;        // (nk_total, 2) column-major, device
+  int nk_total;           // leading dimension of k
+  int k0, kc;             // k chunk [k0, k0+kc)
+  const double2* rab;     // [nRu] (ia, ib) of the used R vectors, device
+  const double2* hr;      // [nRu][nw*nw] column-major blocks, sorted by R3, device
+  const int* icoff;       // [nic+1] offsets of each R3 group in hr, device
+  int ic_lo, nic;         // R3 = ic_lo + group index
+  int nRu, nw, np, ijmax;
+  double2* phase;         // [kc][nRu] scratch
+  double2* h;             // [kc][2][N*N] output: H00 then H01, column-major
+};
+void launch_fourier(const FourierArgs& a, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Lopez-Sancho decimation, all FP64 (surfgreen_1985)
+// ---------------------------------------------------------------------------
+struct DecimArgs {
+  int N, nw;                  // Ndim, Num_wann
+  int nomega;                 // omega points per k
+  int n_inst;                 // instances in this launch: (k chunk) x nomega, omega fastest
+  const double2* h;           // [kc][2][N*N] H00/H01 of the chunk
+  const double* omega;        // [nomega]
+  double eta, tol;
+  int itermax;
+  int divide_by_pi;
+  int nk_total, k_offset;     // output index = (k_offset + ik) + iw * nk_total
+  double* dos_l;
+  double* dos_r;
+  double* dos_bulk;
+  int32_t* iters;             // may be null
+  uint8_t* status;            // may be null
+  double2* gll;               // optional full outputs [n_inst][N*N] (null = skip)
+  double2* grr;
+  double2* gb;
+  double2* ws;                // [grid][8][N*N] workspace
+  int* counter;               // work counter, zero at launch
+  int KC;                     // GEMM k-chunk staged in shared memory
+  int ntop, nbot;
+  int top[MAX_ORB];           // 1-based orbital lists (TopOrbitals / BottomOrbitals)
+  int bot[MAX_ORB];
+};
+
+struct DecimConfig {
+  int threads;
+  int KC;
+  int RP;                     // register rows per pass in the GEMM (template)
+  size_t smem;                // dynamic shared memory per CTA
+  int ctas_per_sm;
+};
+
+// Largest Ndim the shared-memory Gauss-Jordan kernel takes.
+int decim_fp64_max_n();
+// Launch shape for a given N on the current device (threads override: 0 = auto).
+cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg);
+cudaError_t launch_decimate_fp64(const DecimArgs& a, const DecimConfig& cfg, int grid,
+                                 cudaStream_t s);
+
+}  // namespace wtg
