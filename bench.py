@@ -1,0 +1,426 @@
+#!/usr/bin/env python
+"""Surface-GF (k, omega) solves/s on GB300 for WannierTools' SurfaceDOSkk path.
+
+Workload (default): the Fermi-arc plane of a seeded synthetic TaAs-sized
+model, Num_wann = 56, Np = 2 (Ndim = 112), a 201 x 201 k-plane over the full
+surface BZ at omega = 0 with eta = 1e-3 eV, all-FP64, reference convergence
+settings (tol = 1e-16 single-precision literal, itermax = 100).  A step is one
+pass of the hot path (Fourier sum + decimation + spectral sums) over a slab
+of B consecutive k points of the plane; successive steps walk the plane.
+
+Arms:
+  (default)          the GPU path.  `value`: device-resident inputs, timed with
+                     CUDA events on the launching stream; `e2e`: the host-buffer
+                     C-ABI call wtg_surface_spectrum (pinned k list in, dos out);
+                     `cpu_baseline`: the CPU oracle on a bounded sample.
+  --impl reference   the CPU oracle (numpy + LAPACK restatement of the
+                     reference, one process per host core) on the same config.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "surface-GF (k,omega) solves/s"
+EV2HARTREE = 1.0 / 27.211385
+
+WORKLOADS = {
+    # the Fermi-arc plane (SurfaceDOSkk): one omega per k, /pi sums
+    "arc_n112": dict(nw=56, np_=2, seed=2024, nk1=201, nk2=201, omega_ev=[0.0], eta_ev=1e-3,
+                     divide_by_pi=True, tol=None, cpu_per_core=12, ref_per_core=4,
+                     desc="SurfaceDOSkk Fermi-arc plane, synthetic Num_wann=56 Np=2 (Ndim=112), "
+                          "201x201 k-plane, omega=0, eta=1e-3 eV, FP64"),
+    # the k-path x omega spectrum (surfstat): 101 k x 201 omega, eta 1e-2 eV, tol 1e-10
+    "ss_n40": dict(nw=20, np_=2, seed=2023, nk1=101, nk2=None, omega_ev=None, eta_ev=1e-2,
+                   divide_by_pi=False, tol=1e-10, cpu_per_core=1, ref_per_core=1,
+                   desc="surfstat k-path x omega, synthetic Num_wann=20 Np=2 (Ndim=40), "
+                        "101 k x 201 omega in [-1,1] eV, eta=1e-2 eV, tol=1e-10, FP64"),
+}
+
+
+def workload_points(wl: dict):
+    """(k list (nk,2), omega list (Hartree)) of a workload."""
+    import numpy as np
+    from wannier_tools_gb300.api import kpath_slab, kplane_slab
+    if wl["nk2"] is not None:
+        _, _, k = kplane_slab(wl["nk1"], wl["nk2"], (-0.5, -0.5), (1.0, 0.0), (0.0, 1.0))
+        om = np.asarray(wl["omega_ev"]) * EV2HARTREE
+    else:
+        k = kpath_slab([((-0.5, 0.0), (0.5, 0.0))], wl["nk1"])
+        om = np.linspace(-1.0, 1.0, 201) * EV2HARTREE
+    return k, om
+
+
+def orbitals(wl: dict):
+    nw = wl["nw"]
+    return list(range(1, nw + 1)), list(range(1, nw + 1))
+
+
+# --- CPU oracle worker (spawned processes, one BLAS thread each) -------------
+
+_MODEL_CACHE: dict = {}
+
+
+def _cpu_model(wl):
+    from wannier_tools_gb300 import synthetic
+    key = (wl["nw"], wl["np_"], wl["seed"])
+    if key not in _MODEL_CACHE:
+        _MODEL_CACHE[key] = synthetic.make_model(wl["nw"], wl["np_"], seed=wl["seed"])
+    return _MODEL_CACHE[key]
+
+
+def _cpu_warm(wl):
+    _cpu_model(wl)
+    time.sleep(0.2)             # keep this worker busy so every worker gets one warm task
+    return os.getpid()
+
+
+def _cpu_worker(args):
+    import numpy as np
+    from oracle import wt_oracle as O
+    wl, kpts, om = args
+    m = _cpu_model(wl)
+    top, bot = orbitals(wl)
+    tol = wl["tol"] if wl["tol"] is not None else O.ACCURACY_REF
+    t0 = time.perf_counter()
+    O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, m.nw, m.np_, np.asarray(kpts), np.asarray(om),
+                       wl["eta_ev"] * EV2HARTREE, top, bot,
+                       scale=(1.0 / O.PI_REF if wl["divide_by_pi"] else 1.0), accuracy=tol)
+    return time.perf_counter() - t0
+
+
+def cpu_pool(ncores: int):
+    import multiprocessing as mp
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    return mp.get_context("spawn").Pool(ncores)
+
+
+def cpu_sample_rate(pool, ncores: int, wl: dict, per_core: int, offset: int = 0):
+    """Solves/s of the oracle over ncores * per_core k points of the workload,
+    each with all of its omega points (one Fourier sum per k, as the
+    reference's loops do)."""
+    import numpy as np
+    pool.map(_cpu_warm, [wl] * ncores, chunksize=1)
+    k, om = workload_points(wl)
+    nks = ncores * per_core
+    idx = (offset + np.arange(nks) * max(1, len(k) // nks)) % len(k)
+    tasks = [(wl, k[[i]], om) for i in idx]
+    t0 = time.perf_counter()
+    pool.map(_cpu_worker, tasks, chunksize=1)
+    wall = time.perf_counter() - t0
+    npts = nks * len(om)
+    return npts / wall, wall, npts
+
+
+# --- clocks during the timed region -------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sms.append(float(p[1]))
+                maxs.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sms) if sms else None,
+                "sm_max_mhz": max(maxs) if maxs else None, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+# --- arms ---------------------------------------------------------------------
+
+def dist_setup(backend: str):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import wannier_tools_gb300 as w
+    from wannier_tools_gb300 import api
+
+    wl = WORKLOADS[args.workload]
+    ws, rank, local = dist_setup("nccl")
+    pool = None
+    ncores = os.cpu_count() or 1
+    if rank == 0 and not args.no_cpu_baseline:
+        pool = cpu_pool(ncores)               # spawn before the first GPU call
+    torch.cuda.set_device(local)
+    w.build()
+    dev = torch.device("cuda", local)
+
+    m = w.make_model(wl["nw"], wl["np_"], seed=wl["seed"])
+    model = w.Model.from_surface_model(m)
+    k_all, om = workload_points(wl)
+    top, bot = orbitals(wl)
+    nomega = len(om)
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    B = args.batch or (nsm * 8 if nomega == 1 else max(1, (nsm * 8 * 4) // nomega))
+    tol = wl["tol"] if wl["tol"] is not None else api.ACCURACY_REF
+    eta = wl["eta_ev"] * EV2HARTREE
+    nk_total = len(k_all)
+    n_slabs = (nk_total + B - 1) // B
+
+    def slab(step):
+        s = (step * ws + rank) % n_slabs
+        idx = (np.arange(B) + s * B) % nk_total
+        return k_all[idx]
+
+    stream = torch.cuda.current_stream(dev)
+    d_om = torch.tensor(om, dtype=torch.float64, device=dev)
+    slabs = [torch.tensor(np.ascontiguousarray(slab(i).T), dtype=torch.float64, device=dev)
+             for i in range(args.warmup + args.steps)]
+    outs = [torch.empty((nomega, B), dtype=torch.float64, device=dev) for _ in range(3)]
+    nsteps = args.warmup + args.steps
+    d_it = [torch.empty((nomega, B), dtype=torch.int32, device=dev) for _ in range(nsteps)]
+    d_st = [torch.empty((nomega, B), dtype=torch.uint8, device=dev) for _ in range(nsteps)]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)    # > L2 (126 MiB)
+
+    def step(i):
+        flush.zero_()
+        model.surface_spectrum_device(slabs[i], d_om, eta, top, bot, outs[0], outs[1], outs[2],
+                                      d_it[i], d_st[i], tol=tol, divide_by_pi=wl["divide_by_pi"],
+                                      stream=stream.cuda_stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize(dev)
+    fp64_peak = api.fp64_peak_tflops()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    model.profile(True)
+    n3 = float(m.ndim) ** 3
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for i in range(args.warmup, args.warmup + args.steps):
+            step(i)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    prof = model.profile_read()
+    model.profile(False)
+    # algorithmic work of the timed steps: (56 it + 24) Ndim^3 per solve
+    its = np.concatenate([d_it[i].cpu().numpy().ravel() for i in range(args.warmup, nsteps)])
+    st = np.concatenate([d_st[i].cpu().numpy().ravel() for i in range(args.warmup, nsteps)])
+    flops_alg = float(((56.0 * its + 24.0) * n3).sum())
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    solves = ws * args.steps * B * nomega
+    value = solves / (ms_max / 1e3)
+
+    # e2e through the host-buffer C ABI (pinned k list in, dos/iters/status out)
+    kpin = [torch.empty((2, B), dtype=torch.float64).pin_memory().numpy() for _ in range(args.steps)]
+    for i in range(args.steps):
+        kpin[i][:] = slab(args.warmup + i).T
+    hout = {name: torch.empty(B * nomega, dtype=torch.float64).pin_memory().numpy()
+            for name in ("dos_l", "dos_r", "dos_bulk")}
+    hout["iters"] = torch.empty(B * nomega, dtype=torch.int32).pin_memory().numpy()
+    hout["status"] = torch.empty(B * nomega, dtype=torch.uint8).pin_memory().numpy()
+    model.surface_spectrum(None, om, eta, top, bot, tol=tol, divide_by_pi=wl["divide_by_pi"],
+                           kcol=kpin[0], out=hout)              # warm the host-path buffers
+    if ws > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        model.surface_spectrum(None, om, eta, top, bot, tol=tol, divide_by_pi=wl["divide_by_pi"],
+                               kcol=kpin[i], out=hout)
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = solves / float(te.item())
+
+    cpu = None
+    if pool is not None:
+        per_core = args.cpu_sample_per_core
+        rate, wall, npts = cpu_sample_rate(pool, ncores, wl, per_core)
+        cpu = {"value": rate, "unit": "solves/s", "cores": ncores, "kind": "port",
+               "sample": f"{npts} (k,omega) solves: {ncores * per_core} k points of the same "
+                         f"workload x all their omegas, {ncores} spawned processes x 1 OpenBLAS "
+                         f"thread, {wall:.1f} s wall"}
+        pool.close()
+
+    dec_ms_per_launch = prof["decim_ms"] / max(1, prof["decim_launches"])
+    achieved = flops_alg / (prof["decim_ms"] / 1e3) / 1e12 if prof["decim_ms"] > 0 else None
+    traffic = traffic_per_solve(args.workload)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["desc"], "k_points_per_step": B, "omegas_per_k": nomega,
+                       "ndim": m.ndim, "precision": "fp64", "parallelism": f"replicas x{ws} (k slabs)",
+                       "l2": "flushed between steps (256 MiB write)",
+                       "status_flagged_points": int((st != 0).sum()),
+                       "mean_iterations": float(its.mean())},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": B * 2 * 8 + nomega * 8,
+                    "d2h_bytes_per_step": B * nomega * (3 * 8 + 4 + 1)},
+            "gpu_launches": prof["launches"],
+            "roofline": {"bound": "fp64", "kernel": "k_decimate_fp64", "achieved": achieved,
+                         "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": (achieved / fp64_peak) if achieved else None,
+                         "traffic": (traffic * B * nomega) if traffic else None,
+                         "traffic_unit": "bytes per launch",
+                         "peak_source": "FP64 DFMA throughput measured live (wtg_probe_fp64_peak); "
+                                        "FP64 has no tensor-core path faster than DFMA on GB300",
+                         "launch_ms": dec_ms_per_launch,
+                         "work": "(56*it+24)*Ndim^3 flops per solve, it = FP64 iterations"},
+            "fourier_ms_per_step": prof["fourier_ms"] / args.steps,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    model.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def traffic_per_solve(workload: str):
+    """DRAM bytes per solve of the decimation kernel from the committed ncu
+    summary (profiles/k_decimate_fp64_<workload>.md, line 'traffic_bytes_per_solve:')."""
+    p = ROOT / "profiles" / f"k_decimate_fp64_{workload}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_solve:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args):
+    wl = WORKLOADS[args.workload]
+    ws, rank, _ = dist_setup("gloo")
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    ncores = os.cpu_count() or 1
+    pool = cpu_pool(ncores)
+    per_core = args.ref_per_core
+    for i in range(args.warmup):
+        cpu_sample_rate(pool, ncores, wl, per_core, offset=i * 7919)
+    total_pts, total_s = 0, 0.0
+    for i in range(args.steps):
+        _, wall, npts = cpu_sample_rate(pool, ncores, wl, per_core, offset=(args.warmup + i) * 7919)
+        total_pts += npts
+        total_s += wall
+    pool.close()
+    value = total_pts / total_s
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": wl["desc"], "precision": "fp64",
+                       "sample_per_step": f"{ncores * per_core} k points x all omegas"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": ncores, "kind": "port",
+                             "sample": f"{ncores * per_core} k points (x all omegas) per step spread "
+                                       f"over the workload; numpy+OpenBLAS restatement of the reference "
+                                       f"(the Fortran reference cannot be built here), one process "
+                                       f"per core"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="arc_n112")
+    ap.add_argument("--batch", type=int, default=0, help="k points per step (0 = 8 x SMs)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-per-core", type=int, default=0,
+                    help="k points per host core in the cpu_baseline sample (0 = by workload)")
+    ap.add_argument("--ref-per-core", type=int, default=0,
+                    help="k points per host core per reference-arm step (0 = by workload)")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.cpu_sample_per_core <= 0:
+        args.cpu_sample_per_core = wl["cpu_per_core"]
+    if args.ref_per_core <= 0:
+        args.ref_per_core = wl["ref_per_core"]
+    if args.warmup < 3 and args.impl == "ours":
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

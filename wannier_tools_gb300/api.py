@@ -110,18 +110,30 @@ class Model:
     # -- batched spectrum (host buffers) ------------------------------------
     def surface_spectrum(self, kpts, omegas, eta: float, top, bot,
                          tol: float = ACCURACY_REF, itermax: int = ITERMAX_REF,
-                         divide_by_pi: bool = False, precision: int = PREC_FP64) -> dict:
-        """dos_l / dos_r / dos_bulk / iters / status as (nk, nomega) arrays."""
-        kp = np.asarray(kpts, dtype=np.float64).reshape(-1, 2)
-        nk = kp.shape[0]
-        kcol = np.ascontiguousarray(kp.T)                 # (nk, 2) column-major
+                         divide_by_pi: bool = False, precision: int = PREC_FP64,
+                         kcol=None, out: dict | None = None) -> dict:
+        """dos_l / dos_r / dos_bulk / iters / status as (nk, nomega) arrays.
+
+        ``kcol`` may give the k list already in the ABI layout (a contiguous
+        (2, nk) float64 array, e.g. in pinned memory); ``out`` may give
+        preallocated flat host arrays (dos_l, dos_r, dos_bulk float64,
+        iters int32, status uint8, each nk*nomega long)."""
+        if kcol is None:
+            kp = np.asarray(kpts, dtype=np.float64).reshape(-1, 2)
+            kcol = np.ascontiguousarray(kp.T)             # (nk, 2) column-major
+        nk = kcol.shape[1]
         w = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64).ravel())
         nwo = w.shape[0]
         top_a = np.ascontiguousarray(np.asarray(top, dtype=np.int32).ravel())
         bot_a = np.ascontiguousarray(np.asarray(bot, dtype=np.int32).ravel())
-        outs = {name: np.zeros(nk * nwo) for name in ("dos_l", "dos_r", "dos_bulk")}
-        iters = np.zeros(nk * nwo, np.int32)
-        status = np.zeros(nk * nwo, np.uint8)
+        if out is None:
+            outs = {name: np.zeros(nk * nwo) for name in ("dos_l", "dos_r", "dos_bulk")}
+            iters = np.zeros(nk * nwo, np.int32)
+            status = np.zeros(nk * nwo, np.uint8)
+        else:
+            outs = {name: out[name] for name in ("dos_l", "dos_r", "dos_bulk")}
+            iters = out["iters"]
+            status = out["status"]
         check(_lib.load().wtg_surface_spectrum(
             self._handle, nk, _dptr(kcol), nwo, _dptr(w), float(eta), float(tol), int(itermax),
             len(top_a), _iptr(top_a), len(bot_a), _iptr(bot_a), int(bool(divide_by_pi)), precision,
@@ -156,6 +168,23 @@ class Model:
             ptr(d_dos_l), ptr(d_dos_r), ptr(d_dos_bulk), ptr(d_iters), ptr(d_status),
             C.c_void_p(stream)))
 
+
+    # -- tracing -------------------------------------------------------------
+    def profile(self, enable: bool) -> None:
+        """Reset and enable/disable per-launch CUDA-event timing (wtg_model_profile)."""
+        check(_lib.load().wtg_model_profile(self._handle, int(enable)))
+
+    def profile_read(self) -> dict:
+        """Summed device ms of the Fourier and decimation launches since the
+        last reset, and the number of this library's kernels launched."""
+        f = C.c_double(0.0)
+        d = C.c_double(0.0)
+        n = C.c_longlong(0)
+        nd = C.c_int(0)
+        check(_lib.load().wtg_model_profile_read(self._handle, C.byref(f), C.byref(d), C.byref(n),
+                                                 C.byref(nd)))
+        return {"fourier_ms": f.value, "decim_ms": d.value, "launches": int(n.value),
+                "decim_launches": int(nd.value)}
 
 def surfgreen_1985(omega: float, h00: np.ndarray, h01: np.ndarray, eta: float,
                    tol: float = ACCURACY_REF, itermax: int = ITERMAX_REF):
@@ -260,3 +289,11 @@ def arc_post(dos_l, dos_r):
     """src/fermiarc.f90:372-397."""
     return (np.where(dos_l < dos_l.max() / 10.0, EPS9, dos_l),
             np.where(dos_r < dos_r.max() / 10.0, EPS9, dos_r))
+
+
+def fp64_peak_tflops() -> float:
+    """FP64 DFMA throughput of the current GPU (wtg_probe_fp64_peak)."""
+    v = C.c_double(0.0)
+    check(_lib.load().wtg_probe_fp64_peak(C.byref(v)))
+    return float(v.value)
+
