@@ -168,6 +168,32 @@ int wtg_model_profile_read(wtg_model_t model, double* fourier_ms, double* decim_
    denominator of the FP64 path, measured with a short throughput kernel. */
 int wtg_probe_fp64_peak(double* tflops);
 
+/*
+ * Allocation-free batched decimation.  No counterpart in the reference: it
+ * exists for callers that cannot let the library call cudaMalloc -- a host
+ * whose device memory is owned by another allocator (a caching pool that has
+ * reserved the free HBM), or a latency-critical loop where cudaMalloc/cudaFree
+ * would synchronise the device.  Runs the FP64 decimation + spectral sums of
+ * wtg_surface_spectrum_device on H00/H01 the caller already holds on the
+ * device, with all scratch in a fixed 64 MiB device array inside the library
+ * (held on every GPU that loads it, until exit).  Nothing is allocated.
+ *
+ *   ndim, nw   Ndim and Num_wann (ndim a multiple of nw; ndim <= 119, the kernel limit)
+ *   d_h        device complex[nk][2][ndim*ndim]: per k, H00 then H01, column-major
+ *   d_omega    device double[nomega]; outputs device arrays (nk, nomega) column-major
+ *   top/bot    host 1-based orbital lists; stream a cudaStream_t (NULL = default)
+ * Sizes beyond the kernel limit or the fixed scratch return WTG_EUNSUPPORTED.
+ * The first call on a device looks up the scratch address (make it before
+ * any stream capture).  Calls share the scratch: calls that overlap on the
+ * GPU race; the caller orders them (e.g. one stream).
+ */
+int wtg_surfgreen_batch_noalloc(int ndim, int nw, int nk, const double* d_h, int nomega,
+                                const double* d_omega, double eta, double tol, int itermax,
+                                int ntop, const int* top, int nbot, const int* bot,
+                                int divide_by_pi, double* d_dos_l, double* d_dos_r,
+                                double* d_dos_bulk, int32_t* d_iters, uint8_t* d_status,
+                                void* stream);
+
 /* Copy the calling thread's last error message into buf (NUL-terminated). */
 int wtg_last_error(char* buf, int len);
 

@@ -46,6 +46,9 @@ SIGNATURES = {
     "wtg_model_profile": (C.c_int, [_vp, C.c_int]),
     "wtg_model_profile_read": (C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_longlong), _ip]),
     "wtg_probe_fp64_peak": (C.c_int, [_dp]),
+    "wtg_surfgreen_batch_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_double,
+                                               C.c_double, C.c_int, C.c_int, _ip, C.c_int, _ip, C.c_int,
+                                               _vp, _vp, _vp, _vp, _vp, _vp]),
     "wtg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "wtg_device_info": (C.c_int, [C.c_char_p, C.c_int]),
 }

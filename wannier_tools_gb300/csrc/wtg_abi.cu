@@ -61,6 +61,10 @@ constexpr size_t H_CHUNK_BYTES = (size_t)8 << 30;
 
 }  // namespace
 
+namespace wtg {
+void set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace wtg
+
 struct wtg_model {
   int device = 0;
   int nw = 0, nR = 0, np = 0, ijmax = 0, N = 0;

@@ -90,4 +90,7 @@ cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg);
 cudaError_t launch_decimate_fp64(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                  cudaStream_t s);
 
+// Sets the calling thread's message returned by wtg_last_error.
+void set_last_error(const char* msg);
+
 }  // namespace wtg
