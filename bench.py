@@ -32,6 +32,16 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 METRIC = "surface-GF (k,omega) solves/s"
+
+
+def _measured_peaks():
+    try:
+        return json.loads((Path(__file__).resolve().parent / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+MEASURED_PEAKS = _measured_peaks()
 EV2HARTREE = 1.0 / 27.211385
 
 WORKLOADS = {
@@ -93,10 +103,10 @@ def _cpu_worker(args):
     top, bot = orbitals(wl)
     tol = wl["tol"] if wl["tol"] is not None else O.ACCURACY_REF
     t0 = time.perf_counter()
-    O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, m.nw, m.np_, np.asarray(kpts), np.asarray(om),
-                       wl["eta_ev"] * EV2HARTREE, top, bot,
-                       scale=(1.0 / O.PI_REF if wl["divide_by_pi"] else 1.0), accuracy=tol)
-    return time.perf_counter() - t0
+    r = O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, m.nw, m.np_, np.asarray(kpts), np.asarray(om),
+                           wl["eta_ev"] * EV2HARTREE, top, bot,
+                           scale=(1.0 / O.PI_REF if wl["divide_by_pi"] else 1.0), accuracy=tol)
+    return time.perf_counter() - t0, {k: r[k] for k in ("dos_l", "dos_r", "dos_bulk")}
 
 
 def cpu_pool(ncores: int):
@@ -117,10 +127,11 @@ def cpu_sample_rate(pool, ncores: int, wl: dict, per_core: int, offset: int = 0)
     idx = (offset + np.arange(nks) * max(1, len(k) // nks)) % len(k)
     tasks = [(wl, k[[i]], om) for i in idx]
     t0 = time.perf_counter()
-    pool.map(_cpu_worker, tasks, chunksize=1)
+    res = pool.map(_cpu_worker, tasks, chunksize=1)
     wall = time.perf_counter() - t0
     npts = nks * len(om)
-    return npts / wall, wall, npts
+    ref = {name: np.concatenate([r[1][name] for r in res]) for name in ("dos_l", "dos_r", "dos_bulk")}
+    return npts / wall, wall, npts, k[idx], ref
 
 
 # --- clocks during the timed region -------------------------------------------
@@ -196,6 +207,7 @@ def run_gpu(args):
 
     import wannier_tools_gb300 as w
     from wannier_tools_gb300 import api
+    from wannier_tools_gb300._lib import PREC_FP64, PREC_MIXED
 
     wl = WORKLOADS[args.workload]
     ws, rank, local = dist_setup("nccl")
@@ -218,6 +230,8 @@ def run_gpu(args):
     eta = wl["eta_ev"] * EV2HARTREE
     nk_total = len(k_all)
     n_slabs = (nk_total + B - 1) // B
+    nsteps = args.warmup + args.steps
+    n3 = float(m.ndim) ** 3
 
     def slab(step):
         s = (step * ws + rank) % n_slabs
@@ -227,53 +241,11 @@ def run_gpu(args):
     stream = torch.cuda.current_stream(dev)
     d_om = torch.tensor(om, dtype=torch.float64, device=dev)
     slabs = [torch.tensor(np.ascontiguousarray(slab(i).T), dtype=torch.float64, device=dev)
-             for i in range(args.warmup + args.steps)]
+             for i in range(nsteps)]
     outs = [torch.empty((nomega, B), dtype=torch.float64, device=dev) for _ in range(3)]
-    nsteps = args.warmup + args.steps
     d_it = [torch.empty((nomega, B), dtype=torch.int32, device=dev) for _ in range(nsteps)]
     d_st = [torch.empty((nomega, B), dtype=torch.uint8, device=dev) for _ in range(nsteps)]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)    # > L2 (126 MiB)
-
-    def step(i):
-        flush.zero_()
-        model.surface_spectrum_device(slabs[i], d_om, eta, top, bot, outs[0], outs[1], outs[2],
-                                      d_it[i], d_st[i], tol=tol, divide_by_pi=wl["divide_by_pi"],
-                                      stream=stream.cuda_stream)
-
-    for i in range(args.warmup):
-        step(i)
-    torch.cuda.synchronize(dev)
-    fp64_peak = api.fp64_peak_tflops()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize(dev)
-    model.profile(True)
-    n3 = float(m.ndim) ** 3
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for i in range(args.warmup, args.warmup + args.steps):
-            step(i)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-    if ws > 1:
-        torch.distributed.barrier()
-    ms = e0.elapsed_time(e1)
-    prof = model.profile_read()
-    model.profile(False)
-    # algorithmic work of the timed steps: (56 it + 24) Ndim^3 per solve
-    its = np.concatenate([d_it[i].cpu().numpy().ravel() for i in range(args.warmup, nsteps)])
-    st = np.concatenate([d_st[i].cpu().numpy().ravel() for i in range(args.warmup, nsteps)])
-    flops_alg = float(((56.0 * its + 24.0) * n3).sum())
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    solves = ws * args.steps * B * nomega
-    value = solves / (ms_max / 1e3)
-
-    # e2e through the host-buffer C ABI (pinned k list in, dos/iters/status out)
     kpin = [torch.empty((2, B), dtype=torch.float64).pin_memory().numpy() for _ in range(args.steps)]
     for i in range(args.steps):
         kpin[i][:] = slab(args.warmup + i).T
@@ -281,61 +253,141 @@ def run_gpu(args):
             for name in ("dos_l", "dos_r", "dos_bulk")}
     hout["iters"] = torch.empty(B * nomega, dtype=torch.int32).pin_memory().numpy()
     hout["status"] = torch.empty(B * nomega, dtype=torch.uint8).pin_memory().numpy()
-    model.surface_spectrum(None, om, eta, top, bot, tol=tol, divide_by_pi=wl["divide_by_pi"],
-                           kcol=kpin[0], out=hout)              # warm the host-path buffers
-    if ws > 1:
-        torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        flush.zero_()
+
+    def measure(prec):
+        def step(i):
+            flush.zero_()
+            model.surface_spectrum_device(slabs[i], d_om, eta, top, bot, outs[0], outs[1], outs[2],
+                                          d_it[i], d_st[i], tol=tol, divide_by_pi=wl["divide_by_pi"],
+                                          precision=prec, stream=stream.cuda_stream)
+
+        for i in range(args.warmup):
+            step(i)
         torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        model.profile(True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            for i in range(args.warmup, nsteps):
+                step(i)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+        ms = e0.elapsed_time(e1)
+        prof = model.profile_read()
+        model.profile(False)
+        its = np.concatenate([d_it[i].cpu().numpy().ravel() for i in range(args.warmup, nsteps)])
+        st = np.concatenate([d_st[i].cpu().numpy().ravel() for i in range(args.warmup, nsteps)])
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        if ws > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(t.item())
+        solves = ws * args.steps * B * nomega
+        # e2e through the host-buffer C ABI (pinned k list in, dos/iters/status out)
         model.surface_spectrum(None, om, eta, top, bot, tol=tol, divide_by_pi=wl["divide_by_pi"],
-                               kcol=kpin[i], out=hout)
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = solves / float(te.item())
+                               precision=prec, kcol=kpin[0], out=hout)      # warm the host path
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            model.surface_spectrum(None, om, eta, top, bot, tol=tol, divide_by_pi=wl["divide_by_pi"],
+                                   precision=prec, kcol=kpin[i], out=hout)
+        te = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
+        if ws > 1:
+            torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+        return {"value": solves / (ms_max / 1e3), "ms": ms_max, "e2e": solves / float(te.item()),
+                "prof": prof, "its": its, "st": st, "clocks": clk.summary()}
+
+    precs = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+    primary = args.precision
+    forms = [primary] + ([] if args.only else [p for p in ("fp64", "mixed") if p != primary])
+    if m.ndim > 128:
+        forms = [f for f in forms if f != "mixed"]
+    res = {f: measure(precs[f]) for f in forms}
+    fp64_peak = api.fp64_peak_tflops()
 
     cpu = None
+    errors = {}
     if pool is not None:
         per_core = args.cpu_sample_per_core
-        rate, wall, npts = cpu_sample_rate(pool, ncores, wl, per_core)
+        rate, wall, npts, k_sample, oracle_ref = cpu_sample_rate(pool, ncores, wl, per_core)
         cpu = {"value": rate, "unit": "solves/s", "cores": ncores, "kind": "port",
                "sample": f"{npts} (k,omega) solves: {ncores * per_core} k points of the same "
                          f"workload x all their omegas, {ncores} spawned processes x 1 OpenBLAS "
                          f"thread, {wall:.1f} s wall"}
         pool.close()
+        for f in forms:   # max relative error of each form against the FP64 oracle on that sample
+            g = model.surface_spectrum(k_sample, om, eta, top, bot, tol=tol,
+                                       divide_by_pi=wl["divide_by_pi"], precision=precs[f])
+            errors[f] = {name: float(np.max(np.abs(g[name] - oracle_ref[name]) / np.abs(oracle_ref[name])))
+                         for name in ("dos_l", "dos_r", "dos_bulk")}
+            errors[f]["points"] = int(npts)
 
-    dec_ms_per_launch = prof["decim_ms"] / max(1, prof["decim_launches"])
-    achieved = flops_alg / (prof["decim_ms"] / 1e3) / 1e12 if prof["decim_ms"] > 0 else None
-    traffic = traffic_per_solve(args.workload)
+    def roofline(f, r):
+        prof, its = r["prof"], r["its"]
+        launch_ms = prof["decim_ms"] / max(1, prof["decim_launches"])
+        if f == "fp64":
+            flops = float(((56.0 * its + 24.0) * n3).sum())
+            ach = flops / (prof["decim_ms"] / 1e3) / 1e12 if prof["decim_ms"] > 0 else None
+            traffic = traffic_per_solve(args.workload)
+            return {"bound": "fp64", "kernel": "k_decimate_fp64", "achieved": ach, "peak": fp64_peak,
+                    "unit": "TFLOP/s", "frac": (ach / fp64_peak) if ach else None,
+                    "traffic": (traffic * B * nomega) if traffic else None,
+                    "traffic_unit": "bytes per launch",
+                    "peak_source": "FP64 DFMA throughput measured live (wtg_probe_fp64_peak); "
+                                   "FP64 has no tensor-core path faster than DFMA on GB300",
+                    "launch_ms": launch_ms,
+                    "work": "(56*it+24)*Ndim^3 flops per solve, it = FP64 iterations"}
+        npad = (m.ndim + 15) // 16 * 16
+        nch = (m.ndim + 15) // 16
+        per_prod = 2 * nch * 42 * 2.0 * 128 * npad * 16          # BF16 MMA flops of one complex product
+        flops = float(((10.0 * its + 18.0) * per_prod).sum())
+        ach = flops / (prof["decim_ms"] / 1e3) / 1e12 if prof["decim_ms"] > 0 else None
+        peak = MEASURED_PEAKS.get("bf16_tflops")
+        return {"bound": "tensor", "kernel": "k_decimate_mixed", "achieved": ach, "peak": peak,
+                "unit": "TFLOP/s", "frac": (ach / peak) if (ach and peak) else None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)", "launch_ms": launch_ms,
+                "work": "BF16 MMA flops issued: (10*it+18) products per solve x 2 passes x "
+                        "ceil(Ndim/16) chunks x 42 MMAs x 2*128*Ndim16*16",
+                "fp64_equivalent_tflops": float(((56.0 * its + 24.0) * n3).sum()) / (prof["decim_ms"] / 1e3) / 1e12
+                if prof["decim_ms"] > 0 else None}
+
     if rank == 0:
+        r = res[primary]
         line = {
-            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "metric": METRIC, "value": r["value"], "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": wl["desc"], "k_points_per_step": B, "omegas_per_k": nomega,
-                       "ndim": m.ndim, "precision": "fp64", "parallelism": f"replicas x{ws} (k slabs)",
+                       "ndim": m.ndim, "precision": primary,
+                       "parallelism": f"replicas x{ws} (k slabs)",
                        "l2": "flushed between steps (256 MiB write)",
-                       "status_flagged_points": int((st != 0).sum()),
-                       "mean_iterations": float(its.mean())},
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": B * 2 * 8 + nomega * 8,
+                       "status_flagged_points": int((r["st"] != 0).sum()),
+                       "mean_iterations": float(r["its"].mean())},
+            "e2e": {"value": r["e2e"], "unit": "solves/s", "h2d_bytes_per_step": B * 2 * 8 + nomega * 8,
                     "d2h_bytes_per_step": B * nomega * (3 * 8 + 4 + 1)},
-            "gpu_launches": prof["launches"],
-            "roofline": {"bound": "fp64", "kernel": "k_decimate_fp64", "achieved": achieved,
-                         "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": (achieved / fp64_peak) if achieved else None,
-                         "traffic": (traffic * B * nomega) if traffic else None,
-                         "traffic_unit": "bytes per launch",
-                         "peak_source": "FP64 DFMA throughput measured live (wtg_probe_fp64_peak); "
-                                        "FP64 has no tensor-core path faster than DFMA on GB300",
-                         "launch_ms": dec_ms_per_launch,
-                         "work": "(56*it+24)*Ndim^3 flops per solve, it = FP64 iterations"},
-            "fourier_ms_per_step": prof["fourier_ms"] / args.steps,
-            "clocks": clk.summary(),
+            "gpu_launches": r["prof"]["launches"],
+            "roofline": roofline(primary, r),
+            "fourier_ms_per_step": r["prof"]["fourier_ms"] / args.steps,
+            "clocks": r["clocks"],
             "cpu_baseline": cpu,
+            "max_rel_err_vs_fp64_oracle": errors.get(primary),
         }
+        for f in forms[1:]:
+            o = res[f]
+            line[f] = {"value": o["value"], "e2e": o["e2e"], "ms_per_step": o["ms"] / args.steps,
+                       "speedup_vs_" + primary: o["value"] / r["value"],
+                       "gpu_launches": o["prof"]["launches"], "roofline": roofline(f, o),
+                       "mean_iterations": float(o["its"].mean()),
+                       "status_flagged_points": int((o["st"] != 0).sum()),
+                       "max_rel_err_vs_fp64_oracle": errors.get(f), "clocks": o["clocks"]}
         print(json.dumps(line))
     model.close()
     if ws > 1:
@@ -372,7 +424,7 @@ def run_reference(args):
         cpu_sample_rate(pool, ncores, wl, per_core, offset=i * 7919)
     total_pts, total_s = 0, 0.0
     for i in range(args.steps):
-        _, wall, npts = cpu_sample_rate(pool, ncores, wl, per_core, offset=(args.warmup + i) * 7919)
+        _, wall, npts, _, _ = cpu_sample_rate(pool, ncores, wl, per_core, offset=(args.warmup + i) * 7919)
         total_pts += npts
         total_s += wall
     pool.close()
@@ -404,6 +456,9 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="arc_n112")
     ap.add_argument("--batch", type=int, default=0, help="k points per step (0 = 8 x SMs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
+                    help="form reported as `value` (the other is reported beside it)")
+    ap.add_argument("--only", action="store_true", help="time only the --precision form")
     ap.add_argument("--cpu-sample-per-core", type=int, default=0,
                     help="k points per host core in the cpu_baseline sample (0 = by workload)")
     ap.add_argument("--ref-per-core", type=int, default=0,

@@ -53,9 +53,15 @@ extern "C" {
 #define WTG_PT_SINGULAR      2  /* exact zero pivot; the inverse is replaced by the
                                    identity, as zgesv+inv do (src/inverse.f90:51-55) */
 #define WTG_PT_NONFINITE     4  /* a spectral sum is NaN or Inf */
+#define WTG_PT_TIMEOUT       8  /* a bounded wait on the tensor cores gave up (mixed form);
+                                   the point's outputs are not valid */
 
 /* precision modes */
-#define WTG_PREC_FP64  0        /* all-FP64 decimation */
+#define WTG_PREC_FP64  0        /* all-FP64 decimation (FP64 DFMA pipe) */
+#define WTG_PREC_MIXED 1        /* products as exact BF16 digit splits on the tcgen05 tensor
+                                   cores (42-bit operands, FP32 accumulation exact per slice
+                                   order, int64 recombination), inverses FP32 Gauss-Jordan +
+                                   Newton-Schulz refinement on those products; Ndim <= 128 */
 
 typedef struct wtg_model* wtg_model_t;
 
@@ -106,6 +112,17 @@ int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00,
                        int* iters, int* status);
 
 /*
+ * One complex product C = A*B, replacing mat_mul (ZGEMM, src/mat_mul.f90:3-27),
+ * and one inverse A := A^-1 in place, replacing inv (zgesv with an identity
+ * right-hand side, src/inverse.f90:1-58), on the GPU with the decimation's own
+ * device code in either precision.  n x n column-major complex host buffers.
+ * wtg_inv returns 1 (and status PT_SINGULAR) on an exact zero pivot, leaving
+ * the identity as the reference's inv does.
+ */
+int wtg_mat_mul(int n, const double* a, const double* b, double* c, int precision);
+int wtg_inv(int n, double* a, int precision, int* status);
+
+/*
  * Batched surface spectrum over an explicit k list x omega list: for every
  * (k, omega) the Fourier sum of ham_qlayer2qlayer, one surfgreen_1985
  * decimation, and the spectral sums
@@ -122,7 +139,7 @@ int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00,
  *            src/fermiarc.f90:194)
  *   top/bot  1-based orbital lists (TopOrbitals / BottomOrbitals)
  *   divide_by_pi  0 for surfstat, 1 for SurfaceDOSkk
- *   precision     WTG_PREC_FP64
+ *   precision     WTG_PREC_FP64 or WTG_PREC_MIXED
  *   dos_l, dos_r, dos_bulk  double[nk*nomega], column-major (nk, nomega)
  *   iters (int32) / status (uint8) [nk*nomega], optional (NULL)
  * All pointers are host pointers.

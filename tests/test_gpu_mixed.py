@@ -1,0 +1,111 @@
+"""Mixed-precision form: split-BF16 products on the tcgen05 tensor cores.
+
+Checked against numpy (products, inverses) and against the FP64 oracle
+(spectra).  Tolerances: a split product keeps 42 bits per operand against a
+per-row / per-column exponent, so products must match to 1e-10 normwise
+(about 5e-12 expected); Newton-Schulz-refined inverses to 1e-9 normwise;
+the surface / bulk spectral densities to the 1e-5 relative error the mixed
+form is specified for (about 1e-7 expected)."""
+import numpy as np
+import pytest
+
+from oracle import wt_oracle as O
+from wannier_tools_gb300 import api, synthetic
+from wannier_tools_gb300._lib import PREC_FP64, PREC_MIXED
+
+pytestmark = pytest.mark.gpu
+
+EV = O.EV2HARTREE
+
+
+def crand(rng, n, m=None):
+    m = m or n
+    return rng.normal(size=(n, m)) + 1j * rng.normal(size=(n, m))
+
+
+def nrel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("n", [1, 8, 17, 40, 64, 112, 128])
+def test_mat_mul_both_precisions(built_lib, n):
+    rng = np.random.default_rng(n)
+    a, b = crand(rng, n), crand(rng, n)
+    ref = a @ b
+    if n <= 119:                      # the FP64 kernel's shared-memory limit
+        assert nrel(api.mat_mul(a, b, PREC_FP64), ref) <= 1e-14
+    assert nrel(api.mat_mul(a, b, PREC_MIXED), ref) <= 1e-10
+
+
+def test_mat_mul_mixed_wide_dynamic_range(built_lib):
+    """Rows of A and columns of B scaled over 1e-12..1e12: each output element
+    keeps its accuracy relative to its own row/column scale."""
+    rng = np.random.default_rng(5)
+    n = 48
+    ra = 10.0 ** rng.uniform(-12, 12, n)
+    cb = 10.0 ** rng.uniform(-12, 12, n)
+    a = crand(rng, n) * ra[:, None]
+    b = crand(rng, n) * cb[None, :]
+    got = api.mat_mul(a, b, PREC_MIXED)
+    ref = a @ b
+    scale = np.outer(ra, cb) * n
+    assert np.max(np.abs(got - ref) / scale) <= 1e-10
+
+
+@pytest.mark.parametrize("n", [1, 5, 40, 112, 128])
+def test_inverse_both_precisions(built_lib, n):
+    rng = np.random.default_rng(100 + n)
+    a = crand(rng, n) + 3.0 * np.sqrt(n) * np.eye(n)
+    ref = np.linalg.inv(a)
+    if n <= 119:
+        g64, st64 = api.inv(a, PREC_FP64)
+        assert st64 == 0 and nrel(g64, ref) <= 1e-13
+    gmx, stmx = api.inv(a, PREC_MIXED)
+    assert stmx == 0 and nrel(gmx, ref) <= 1e-9
+
+
+def test_inverse_near_pole(built_lib):
+    """w - H00 one micro-Hartree from an eigenvalue, eta = 1e-4 eV (condition ~1e6)."""
+    m = synthetic.make_model(20, 2, seed=3)
+    h00, _ = O.ham_qlayer2qlayer([0.1, 0.2], m.hmnr, m.irvec, m.ndegen, 20, 2)
+    ev = np.linalg.eigvalsh(h00)
+    w = complex(ev[17] + 1e-6, 1e-4 * EV)
+    a = w * np.eye(40) - h00
+    ref = np.linalg.inv(a)
+    gmx, st = api.inv(a, PREC_MIXED)
+    # 42-bit split products: normwise error ~ 2^-42 x condition number (~1e6 here)
+    assert st == 0 and nrel(gmx, ref) <= 1e-12 * np.linalg.cond(a)
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+@pytest.mark.parametrize("nw,np_,eta_ev,oms,arc", [
+    (20, 2, 1e-2, [-0.6, 0.0, 0.45], False),    # surfstat shape, Ndim 40
+    (56, 2, 1e-3, [0.0], True),                  # Fermi-arc shape, Ndim 112
+    (8, 2, 1e-4, [0.0, 0.7], False),             # small eta, Ndim 16
+    (44, 3, 1e-3, [0.05], False),                # Np = 3, Ndim 132 > 128: rejected
+])
+def test_spectrum_mixed_vs_fp64_oracle(built_lib, nw, np_, eta_ev, oms, arc):
+    from wannier_tools_gb300._lib import WtgError
+    m = synthetic.make_model(nw, np_, seed=nw + np_)
+    kp = synthetic.random_kpoints(3, seed=nw)
+    om = np.asarray(oms) * EV
+    top = list(range(1, nw + 1, 2))
+    bot = list(range(2, nw + 1, 3))
+    with api.Model.from_surface_model(m) as g:
+        if nw * np_ > 128:
+            with pytest.raises(WtgError):
+                g.surface_spectrum(kp, om, eta_ev * EV, top, bot, precision=PREC_MIXED)
+            return
+        got = g.surface_spectrum(kp, om, eta_ev * EV, top, bot, divide_by_pi=arc,
+                                 precision=PREC_MIXED)
+    ref = O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, nw, np_, kp, om, eta_ev * EV, top, bot,
+                             scale=(1.0 / O.PI_REF if arc else 1.0))
+    errs = {name: _rel(got[name], ref[name]) for name in ("dos_l", "dos_r", "dos_bulk")}
+    print("mixed max rel err", nw, np_, eta_ev, errs)
+    for name, e in errs.items():
+        assert e <= 1e-5, (name, e)
+    assert np.abs(got["iters"] - ref["iters"]).max() <= 1
+    assert (got["status"] == 0).all()

@@ -20,8 +20,10 @@ WTG_EUNSUPPORTED = -6
 PT_NOT_CONVERGED = 1
 PT_SINGULAR = 2
 PT_NONFINITE = 4
+PT_TIMEOUT = 8
 
 PREC_FP64 = 0
+PREC_MIXED = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -43,6 +45,8 @@ SIGNATURES = {
     "wtg_surface_spectrum_device": (C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_double, C.c_double,
                                                C.c_int, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int,
                                                _vp, _vp, _vp, _vp, _vp, _vp]),
+    "wtg_mat_mul": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int]),
+    "wtg_inv": (C.c_int, [C.c_int, _dp, C.c_int, _ip]),
     "wtg_model_profile": (C.c_int, [_vp, C.c_int]),
     "wtg_model_profile_read": (C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_longlong), _ip]),
     "wtg_probe_fp64_peak": (C.c_int, [_dp]),

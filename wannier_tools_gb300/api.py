@@ -24,7 +24,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import PREC_FP64, check
+from ._lib import PREC_FP64, PREC_MIXED, check  # noqa: F401
 
 PI_REF = 3.14159265358979                    # src/module.f90:719
 EV2HARTREE = 1.0 / 27.211385                 # src/module.f90:713
@@ -203,6 +203,26 @@ def surfgreen_1985(omega: float, h00: np.ndarray, h01: np.ndarray, eta: float,
                                          _dptr(gb.view(np.float64)), C.byref(it), C.byref(st)))
     return (_from_colmajor(gll, n), _from_colmajor(grr, n), _from_colmajor(gb, n),
             int(it.value), int(st.value))
+
+
+def mat_mul(a: np.ndarray, b: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:
+    """C = A*B on the GPU (mat_mul, src/mat_mul.f90:3-27)."""
+    n = a.shape[0]
+    x = _to_colmajor(a)
+    y = _to_colmajor(b)
+    c = np.empty(n * n, np.complex128)
+    check(_lib.load().wtg_mat_mul(n, _dptr(x.view(np.float64)), _dptr(y.view(np.float64)),
+                                  _dptr(c.view(np.float64)), precision))
+    return _from_colmajor(c, n)
+
+
+def inv(a: np.ndarray, precision: int = PREC_FP64):
+    """A^-1 on the GPU (inv, src/inverse.f90:1-58): (inverse, status)."""
+    n = a.shape[0]
+    x = _to_colmajor(a).copy()
+    st = C.c_int(0)
+    check(_lib.load().wtg_inv(n, _dptr(x.view(np.float64)), precision, C.byref(st)))
+    return _from_colmajor(x, n), int(st.value)
 
 
 def device_info() -> str:

@@ -98,16 +98,24 @@ namespace {
 
 int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const double* d_omega,
                  double eta, double tol, int itermax, int ntop, const int* top, int nbot,
-                 const int* bot, int divide_by_pi, double* d_dl, double* d_dr, double* d_db,
-                 int32_t* d_it, uint8_t* d_st, cudaStream_t s) {
+                 const int* bot, int divide_by_pi, int precision, double* d_dl, double* d_dr,
+                 double* d_db, int32_t* d_it, uint8_t* d_st, cudaStream_t s) {
   const int N = m->N;
-  if (N > wtg::decim_fp64_max_n())
-    return fail(WTG_EUNSUPPORTED, "Ndim " + std::to_string(N) + " exceeds the FP64 kernel limit " +
-                                      std::to_string(wtg::decim_fp64_max_n()));
+  const bool mixed = precision == WTG_PREC_MIXED;
+  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_max_n();
+  if (N > nmax)
+    return fail(WTG_EUNSUPPORTED, "Ndim " + std::to_string(N) + " exceeds the " +
+                                      (mixed ? "mixed" : "FP64") + " kernel limit " +
+                                      std::to_string(nmax));
   wtg::DecimConfig cfg;
   int thr = 0;
   if (const char* env = getenv("WTG_DECIM_THREADS")) thr = atoi(env);
-  WTG_CK(wtg::decim_fp64_config(N, thr, &cfg));
+  if (mixed) {
+    WTG_CK(wtg::decim_mixed_config(N, &cfg));
+  } else {
+    WTG_CK(wtg::decim_fp64_config(N, thr, &cfg));
+  }
+  const size_t ws_mats = mixed ? wtg::decim_mixed_ws_matrices() : 8;
   if (cfg.ctas_per_sm < 1) return fail(WTG_EUNSUPPORTED, "decimation kernel does not fit an SM");
   int nsm = 0;
   WTG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, m->device));
@@ -121,7 +129,7 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
 
   WTG_CK(m->phase.ensure(sizeof(double2) * (size_t)kchunk * std::max(1, m->nRu)));
   WTG_CK(m->h.ensure(hk * kchunk));
-  WTG_CK(m->ws.ensure(sizeof(double2) * 8 * (size_t)N * N * grid));
+  WTG_CK(m->ws.ensure(sizeof(double2) * ws_mats * (size_t)N * N * grid));
   WTG_CK(m->counter.ensure(sizeof(int) * 64));
 
   WTG_CK(cudaStreamWaitEvent(s, m->done, 0));
@@ -184,7 +192,11 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
     const int g = (int)std::min<long long>(grid, a.n_inst);
     const size_t de0 = m->ev_used;
     if (m->profile) WTG_CK(cudaEventRecord(m->next_event(), s));
-    WTG_CK(wtg::launch_decimate_fp64(a, cfg, g, s));
+    if (mixed) {
+      WTG_CK(wtg::launch_decimate_mixed(a, cfg, g, s));
+    } else {
+      WTG_CK(wtg::launch_decimate_fp64(a, cfg, g, s));
+    }
     m->launches += 1;
     if (m->profile) {
       WTG_CK(cudaEventRecord(m->next_event(), s));
@@ -433,7 +445,8 @@ int wtg_surface_spectrum_device(wtg_model_t m, int nk, const double* d_k, int no
                                 void* stream) {
   if (!m) return fail(WTG_EINVAL, "null model");
   if (nk < 0 || nomega < 0 || itermax < 0) return fail(WTG_EINVAL, "negative size");
-  if (precision != WTG_PREC_FP64) return fail(WTG_EUNSUPPORTED, "precision mode not built");
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
   if (nk == 0 || nomega == 0) return WTG_OK;
   if (!d_k || !d_omega || !d_dos_l || !d_dos_r || !d_dos_bulk) return fail(WTG_EINVAL, "null array");
   int rc = check_lists(m->nw, ntop, top, nbot, bot);
@@ -441,7 +454,7 @@ int wtg_surface_spectrum_device(wtg_model_t m, int nk, const double* d_k, int no
   std::lock_guard<std::mutex> lk(m->mu);
   WTG_CK(cudaSetDevice(m->device));
   return run_spectrum(m, nk, d_k, nomega, d_omega, eta, tol, itermax, ntop, top, nbot, bot,
-                      divide_by_pi, d_dos_l, d_dos_r, d_dos_bulk, d_iters, d_status,
+                      divide_by_pi, precision, d_dos_l, d_dos_r, d_dos_bulk, d_iters, d_status,
                       (cudaStream_t)stream);
 }
 
@@ -451,7 +464,8 @@ int wtg_surface_spectrum(wtg_model_t m, int nk, const double* k, int nomega, con
                          double* dos_r, double* dos_bulk, int32_t* iters, uint8_t* status) {
   if (!m) return fail(WTG_EINVAL, "null model");
   if (nk < 0 || nomega < 0 || itermax < 0) return fail(WTG_EINVAL, "negative size");
-  if (precision != WTG_PREC_FP64) return fail(WTG_EUNSUPPORTED, "precision mode not built");
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
   if (nk == 0 || nomega == 0) return WTG_OK;
   if (!k || !omega || !dos_l || !dos_r || !dos_bulk) return fail(WTG_EINVAL, "null array");
   int rc = check_lists(m->nw, ntop, top, nbot, bot);
@@ -470,7 +484,8 @@ int wtg_surface_spectrum(wtg_model_t m, int nk, const double* k, int nomega, con
   WTG_CK(cudaMemcpyAsync(m->w_in.p, omega, sizeof(double) * nomega, cudaMemcpyHostToDevice, s));
   double* dd = (double*)m->out_dos.p;
   rc = run_spectrum(m, nk, (const double*)m->k_in.p, nomega, (const double*)m->w_in.p, eta, tol,
-                    itermax, ntop, top, nbot, bot, divide_by_pi, dd, dd + npts, dd + 2 * npts,
+                    itermax, ntop, top, nbot, bot, divide_by_pi, precision, dd, dd + npts,
+                    dd + 2 * npts,
                     (int32_t*)m->out_it.p, (uint8_t*)m->out_st.p, s);
   if (rc != WTG_OK) return rc;
   WTG_CK(cudaMemcpyAsync(dos_l, dd, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
@@ -487,6 +502,47 @@ int wtg_surface_spectrum(wtg_model_t m, int nk, const double* k, int nomega, con
     WTG_CK(cudaMemcpyAsync(iters, m->out_it.p, sizeof(int32_t) * npts, cudaMemcpyDeviceToHost, s));
   WTG_CK(cudaStreamSynchronize(s));
   return count_flagged(st_host, npts);
+}
+
+static int unit_op(int op, int n, const double* a, const double* b, double* c, int precision,
+                   int* status) {
+  if (n < 1 || !a || !c || (op == 0 && !b)) return fail(WTG_EINVAL, "bad argument");
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
+  const bool mixed = precision == WTG_PREC_MIXED;
+  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_max_n();
+  if (n > nmax) return fail(WTG_EUNSUPPORTED, "n exceeds the kernel limit " + std::to_string(nmax));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(WTG_ENODEV, "no CUDA device available");
+  const size_t nn = (size_t)n * n;
+  char* base = nullptr;
+  WTG_CK(cudaMalloc(&base, sizeof(double2) * 8 * nn + 64));
+  double2* dx = (double2*)base;
+  double2* dy = dx + nn;
+  double2* dc = dy + nn;
+  double2* dws = dc + nn;            // 5 nn
+  int* dst = (int*)(dws + 5 * nn);
+  cudaError_t e = cudaMemcpy(dx, a, sizeof(double2) * nn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && op == 0) e = cudaMemcpy(dy, b, sizeof(double2) * nn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = mixed ? wtg::launch_mixed_unit(op, n, dx, dy, dc, dws, 3, dst, 0)
+              : wtg::launch_fp64_unit(op, n, dx, dy, dc, dws, dst, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(c, dc, sizeof(double2) * nn, cudaMemcpyDeviceToHost);
+  int st = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(base);
+  if (e != cudaSuccess) return cuda_fail(e, op == 0 ? "wtg_mat_mul" : "wtg_inv");
+  if (status) *status = st;
+  return st ? 1 : WTG_OK;
+}
+
+int wtg_mat_mul(int n, const double* a, const double* b, double* c, int precision) {
+  return unit_op(0, n, a, b, c, precision, nullptr);
+}
+
+int wtg_inv(int n, double* a, int precision, int* status) {
+  return unit_op(1, n, a, nullptr, a, precision, status);
 }
 
 int wtg_model_profile(wtg_model_t m, int enable) {

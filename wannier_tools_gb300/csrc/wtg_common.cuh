@@ -16,6 +16,7 @@ constexpr int MAX_ORB = 1024;     // longest top / bottom orbital list per launc
 constexpr int PT_NOT_CONVERGED = 1;
 constexpr int PT_SINGULAR = 2;
 constexpr int PT_NONFINITE = 4;
+constexpr int PT_TIMEOUT_BIT = 8;
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
@@ -89,6 +90,21 @@ int decim_fp64_max_n();
 cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg);
 cudaError_t launch_decimate_fp64(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                  cudaStream_t s);
+
+// Mixed-precision (split BF16 on tcgen05) decimation; same arguments, workspace of
+// decim_mixed_ws_matrices() N x N complex matrices per CTA.
+int decim_mixed_max_n();
+size_t decim_mixed_ws_matrices();
+cudaError_t decim_mixed_config(int N, DecimConfig* cfg);
+cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
+                                  cudaStream_t s);
+
+// One product (op 0: C = X*Y) or inverse (op 1: C = X^-1) by a single CTA.
+// Mixed: ws holds 5 N x N complex matrices; FP64: negX holds one.
+cudaError_t launch_mixed_unit(int op, int N, const double2* X, const double2* Y, double2* C,
+                              double2* ws, int ns, int* status, cudaStream_t s);
+cudaError_t launch_fp64_unit(int op, int N, const double2* X, const double2* Y, double2* C,
+                             double2* negX, int* status, cudaStream_t s);
 
 // Sets the calling thread's message returned by wtg_last_error.
 void set_last_error(const char* msg);

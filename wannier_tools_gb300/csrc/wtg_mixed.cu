@@ -1,0 +1,829 @@
+// Mixed-precision Lopez-Sancho decimation on the 5th-generation tensor cores.
+//
+// Every complex product of surfgreen_1985 (src/surfgreen.f90:92-116, zgemm at
+// src/mat_mul.f90:23) runs as an exactly-split BF16 product on tcgen05:
+//   * each FP64 operand is written as 42-bit fixed point against a shared
+//     exponent per row (left factor) or per column (right factor) and cut into
+//     six 7-bit digits; a digit is an exact BF16 value (with a power-of-two
+//     scale folded in);
+//   * slice products A^p B^q with p + q <= 7 are issued as BF16 MMAs with FP32
+//     accumulators in tensor memory, one accumulator per slice order
+//     t = p + q for t = 2, 3, 4 (sums of at most 3 * 2K digit products stay
+//     below 2^24, so these accumulations are exact) and one for t >= 5 (rounded
+//     at 2^-45 of the result);
+//   * the four accumulators are read back (tcgen05.ld), converted to integers
+//     and summed in int64, and the FP64 result is assembled with integer
+//     operations (no FP64 arithmetic for the product itself).
+// The complex product is two passes: Cr = Xr Yr - Xi Yi (the second term via
+// the instruction's negate-B bit) and Ci = Xr Yi + Xi Yr.
+// Inverses (zgesv with identity, src/inverse.f90:43-55) are a shared-memory
+// FP32 Gauss-Jordan followed by Newton-Schulz refinement X <- X + X (I - M X)
+// whose two products are the split products above, so the inverse reaches the
+// products' accuracy.  Convergence test sum |alpha_ij| (src/surfgreen.f90:120)
+// is evaluated in FP32 from the assembled values.
+//
+// Operands are staged per K chunk of 16 (one MMA k-step) into a double-buffered
+// shared-memory area in the canonical K-major, no-swizzle layout (8 x 16-byte
+// core matrices; K-adjacent core matrices 128 B apart, 8-row groups 256 B
+// apart), generated by all threads while the tensor core works on the other
+// buffer; one thread issues the MMAs and commits them to an mbarrier per buffer.
+// Every mbarrier wait is bounded; on a timeout the CTA stops issuing work,
+// marks the instance, waits (bounded) for its MMAs and frees tensor memory.
+#include <cuda_bf16.h>
+
+#include "wtg_common.cuh"
+
+namespace wtg {
+
+namespace {
+
+#include "wtg_fp64_dev.cuh"
+
+constexpr int MX_T = 256;            // threads per CTA (8 warps)
+constexpr int NSL = 6;               // digits per operand
+constexpr int KCH = 16;              // K per staged chunk
+constexpr int APLANE = 128 * KCH * 2;  // bytes of one A plane (128 rows x 16 bf16)
+constexpr unsigned SPIN_LIMIT = 1u << 22;
+constexpr int PT_TIMEOUT = 8;
+
+constexpr int OZ_STORE = 0, OZ_ADD2 = 1, OZ_STORE_NORM = 2, OZ_IMINUS = 3, OZ_ADDTO = 4;
+
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle, LBO 128 B (K), SBO 256 B (rows)
+__device__ __forceinline__ uint64_t sdesc(uint32_t a) {
+  return (uint64_t)((a >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
+         ((uint64_t)(256 >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor: kind::f16, BF16 x BF16 -> FP32, K-major A and B, M = 128
+__device__ __forceinline__ uint32_t idesc(int n, int negb) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)negb << 14) |
+         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t id,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* mb) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   saddr(mb))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* mb, uint32_t parity) {
+  const uint32_t a = saddr(mb);
+  for (unsigned spin = 0; spin < SPIN_LIMIT; ++spin) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// ---- integer-only conversions ---------------------------------------------
+
+__device__ __forceinline__ int bexp(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+// |x| as 42-bit fixed point against biased exponent E (|x| < 2^(E-1022))
+__device__ __forceinline__ unsigned long long fixed42(double x, int E, unsigned& neg) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  neg = (unsigned)(u >> 63);
+  int ex = (int)((u >> 52) & 0x7FF);
+  unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+  if (ex) m |= 1ull << 52;
+  else ex = 1;
+  const int sh = E - ex + 11;
+  return sh < 64 ? (m >> sh) : 0ull;
+}
+
+// BF16 bits of sign * d * 2^s for a 7-bit digit d
+__device__ __forceinline__ uint32_t bf16_digit(uint32_t d, int s, uint32_t neg) {
+  if (d == 0) return 0u;
+  const int L = 31 - __clz(d);
+  const uint32_t mant = (d << (7 - L)) & 0x7Fu;
+  const uint32_t e = (uint32_t)(127 + L + s);
+  return (neg << 15) | (e << 7) | mant;
+}
+
+// integer value of an integer-valued float
+__device__ __forceinline__ long long f2ll_int(uint32_t w) {
+  const int e = (int)((w >> 23) & 0xFF);
+  if (e < 127) return 0;
+  const long long m = (long long)((w & 0x7FFFFFu) | 0x800000u);
+  const int sh = e - 150;
+  const long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
+  return (w >> 31) ? -v : v;
+}
+
+// double with value S * 2^(be0 - 1023) assembled from bits (truncating)
+__device__ __forceinline__ double assemble(long long S, int be0) {
+  if (S == 0) return 0.0;
+  const unsigned long long neg = S < 0 ? 1ull : 0ull;
+  const unsigned long long a = neg ? (unsigned long long)(-S) : (unsigned long long)S;
+  const int L = 63 - __clzll((long long)a);
+  const unsigned long long mant = L >= 52 ? (a >> (L - 52)) : (a << (52 - L));
+  const int be = L + be0;
+  if (be <= 0) return 0.0;
+  if (be >= 2047) return __longlong_as_double((long long)((neg << 63) | (0x7FFull << 52)));
+  return __longlong_as_double(
+      (long long)((neg << 63) | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+__device__ __forceinline__ float d2f_bits(double x) {    // truncating FP64 -> FP32
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const uint32_t sign = (uint32_t)(u >> 63) << 31;
+  const int ex = (int)((u >> 52) & 0x7FF);
+  const int e32 = ex - 1023 + 127;
+  if (ex == 0 || e32 <= 0) return __uint_as_float(sign);
+  if (e32 >= 255) return __uint_as_float(sign | 0x7F800000u);
+  return __uint_as_float(sign | ((uint32_t)e32 << 23) | (uint32_t)((u >> 29) & 0x7FFFFFu));
+}
+
+__device__ __forceinline__ double f2d_bits(float f) {     // exact FP32 -> FP64
+  const uint32_t w = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(w >> 31) << 63;
+  const int e = (int)((w >> 23) & 0xFF);
+  if (e == 0) return __longlong_as_double((long long)sign);
+  if (e == 255) return __longlong_as_double((long long)(sign | (0x7FFull << 52)));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) |
+                  ((unsigned long long)(w & 0x7FFFFFu) << 29)));
+}
+
+// ---- shared state ------------------------------------------------------------
+
+struct MxShared {
+  unsigned char* buf[2];   // per buffer: 12 A planes then 12 B planes
+  float2* gj;              // FP32 Gauss-Jordan matrix (aliases the buffers)
+  float2* colbuf;
+  float2* rowbuf;
+  float2* recip;
+  int* perm;
+  int* cols;
+  int* expA;               // [128]
+  int* expB;               // [128]
+  float* red;              // [32]
+  uint64_t* mbar;          // [2]
+  uint32_t* tslot;
+  int* misc;               // 0 instance, 1 singular, 2 abort
+};
+
+struct MxState {           // per-thread copies of the (uniform) pipeline counters
+  uint32_t tmem;
+  uint32_t ncommit[2];
+  uint32_t nwaited[2];
+  int abort;
+};
+
+__device__ __forceinline__ void buffer_ready(MxShared& s, MxState& st, int b) {
+  if (st.ncommit[b] > st.nwaited[b]) {
+    if (!mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1)) st.abort = 1;
+    st.nwaited[b] = st.ncommit[b];
+  }
+}
+
+// row exponents of X (over re and im), column exponents of Y
+__device__ void oz_exponents(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
+                             MxShared& s) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int r = warp; r < 2 * N; r += nwarp) {
+    int mx = 0;
+    if (r < N) {
+      for (int k = lane; k < N; k += 32) {
+        const double2 v = X[r + (size_t)k * N];
+        mx = max(mx, max(bexp(v.x), bexp(v.y)));
+      }
+    } else {
+      const int j = r - N;
+      for (int k = lane; k < N; k += 32) {
+        const double2 v = Y[k + (size_t)j * N];
+        mx = max(mx, max(bexp(v.x), bexp(v.y)));
+      }
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0) {
+      if (r < N) s.expA[r] = mx;
+      else s.expB[r - N] = mx;
+    }
+  }
+}
+
+// digit planes of chunk [k0, k0+16) into buffer b
+__device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
+                            int NP, int k0, const MxShared& s, int b) {
+  unsigned char* A = s.buf[b];
+  unsigned char* B = A + 2 * NSL * APLANE;
+  const int bplane = NP * KCH * 2;
+  for (int it = threadIdx.x; it < 128 * (KCH / 2); it += blockDim.x) {
+    const int i = it & 127, kk = 2 * (it >> 7);
+    double2 x0 = make_double2(0.0, 0.0), x1 = x0;
+    int E = 0;
+    if (i < N) {
+      E = s.expA[i];
+      if (k0 + kk < N) x0 = X[i + (size_t)(k0 + kk) * N];
+      if (k0 + kk + 1 < N) x1 = X[i + (size_t)(k0 + kk + 1) * N];
+    }
+    unsigned n0r, n0i, n1r, n1i;
+    const unsigned long long f0r = fixed42(x0.x, E, n0r), f0i = fixed42(x0.y, E, n0i);
+    const unsigned long long f1r = fixed42(x1.x, E, n1r), f1i = fixed42(x1.y, E, n1i);
+    const int off = (((i >> 3) * 2 + (kk >> 3)) * 64 + (i & 7) * 8 + (kk & 7)) * 2;
+#pragma unroll
+    for (int p = 1; p <= NSL; ++p) {
+      const int sh = 7 * (NSL - p), sc = 7 * (3 - p);
+      const uint32_t wr = bf16_digit((uint32_t)(f0r >> sh) & 127u, sc, n0r) |
+                          (bf16_digit((uint32_t)(f1r >> sh) & 127u, sc, n1r) << 16);
+      const uint32_t wi = bf16_digit((uint32_t)(f0i >> sh) & 127u, sc, n0i) |
+                          (bf16_digit((uint32_t)(f1i >> sh) & 127u, sc, n1i) << 16);
+      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1)) * APLANE + off) = wr;
+      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1) + 1) * APLANE + off) = wi;
+    }
+  }
+  for (int it = threadIdx.x; it < NP * (KCH / 2); it += blockDim.x) {
+    const int kk = 2 * (it & 7), j = it >> 3;
+    double2 y0 = make_double2(0.0, 0.0), y1 = y0;
+    int F = 0;
+    if (j < N) {
+      F = s.expB[j];
+      if (k0 + kk < N) y0 = Y[(k0 + kk) + (size_t)j * N];
+      if (k0 + kk + 1 < N) y1 = Y[(k0 + kk + 1) + (size_t)j * N];
+    }
+    unsigned n0r, n0i, n1r, n1i;
+    const unsigned long long f0r = fixed42(y0.x, F, n0r), f0i = fixed42(y0.y, F, n0i);
+    const unsigned long long f1r = fixed42(y1.x, F, n1r), f1i = fixed42(y1.y, F, n1i);
+    const int off = (((j >> 3) * 2 + (kk >> 3)) * 64 + (j & 7) * 8 + (kk & 7)) * 2;
+#pragma unroll
+    for (int q = 1; q <= NSL; ++q) {
+      const int sh = 7 * (NSL - q), sc = 7 * (4 - q);
+      const uint32_t wr = bf16_digit((uint32_t)(f0r >> sh) & 127u, sc, n0r) |
+                          (bf16_digit((uint32_t)(f1r >> sh) & 127u, sc, n1r) << 16);
+      const uint32_t wi = bf16_digit((uint32_t)(f0i >> sh) & 127u, sc, n0i) |
+                          (bf16_digit((uint32_t)(f1i >> sh) & 127u, sc, n1i) << 16);
+      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1)) * bplane + off) = wr;
+      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1) + 1) * bplane + off) = wi;
+    }
+  }
+}
+
+// all slice-pair MMAs of one chunk (thread 0 only)
+__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int pass, bool first) {
+  const uint32_t A = saddr(s.buf[b]);
+  const uint32_t B = A + 2 * NSL * APLANE;
+  const uint32_t bplane = (uint32_t)NP * KCH * 2;
+  bool started[4] = {false, false, false, false};
+#pragma unroll 1
+  for (int p = 1; p <= NSL; ++p) {
+#pragma unroll 1
+    for (int q = 1; q + p <= NSL + 1; ++q) {
+      const int t = p + q;
+      const int a = t <= 4 ? t - 2 : 3;
+      const uint32_t d = tmem + (uint32_t)(a * NP);
+      const uint32_t aR = A + (uint32_t)(2 * (p - 1)) * APLANE, aI = aR + APLANE;
+      const uint32_t bR = B + (uint32_t)(2 * (q - 1)) * bplane, bI = bR + bplane;
+      const uint32_t acc = (first && !started[a]) ? 0u : 1u;
+      started[a] = true;
+      if (pass == 0) {          // Cr = Xr Yr - Xi Yi
+        mma_bf16(d, sdesc(aR), sdesc(bR), idesc(NP, 0), acc);
+        mma_bf16(d, sdesc(aI), sdesc(bI), idesc(NP, 1), 1u);
+      } else {                  // Ci = Xr Yi + Xi Yr
+        mma_bf16(d, sdesc(aR), sdesc(bI), idesc(NP, 0), acc);
+        mma_bf16(d, sdesc(aI), sdesc(bR), idesc(NP, 0), 1u);
+      }
+    }
+  }
+}
+
+// C = X * Y through the epilogue; returns this thread's FP32 partial of sum |C|
+// (OZ_STORE_NORM only).  out0/out1/src: FP64 N x N column-major.
+template <int EPI>
+__device__ float oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
+                         int NP, double2* out0, double2* out1, const double2* src, MxShared& s,
+                         MxState& st) {
+  const int tid = threadIdx.x;
+  const int nch = (N + KCH - 1) / KCH;
+  float nrm = 0.f;
+  oz_exponents(X, Y, N, s);
+  __syncthreads();
+  for (int pass = 0; pass < 2 && !st.abort; ++pass) {
+    for (int c = 0; c < nch; ++c) {
+      const int b = c & 1;
+      buffer_ready(s, st, b);
+      oz_generate(X, Y, N, NP, c * KCH, s, b);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc_fence_before();
+      st.abort = __syncthreads_or(st.abort);
+      tc_fence_after();
+      if (st.abort) break;
+      if (tid == 0) {
+        oz_issue(s, st.tmem, b, NP, pass, c == 0);
+        mma_commit(&s.mbar[b]);
+      }
+      st.ncommit[b] += 1;
+    }
+    // all MMAs of this pass: the last commit covers every earlier one
+    const int bl = (nch - 1) & 1;
+    if (!st.abort && !mbar_wait(&s.mbar[bl], (st.ncommit[bl] - 1) & 1)) st.abort = 1;
+    if (!st.abort) {
+      st.nwaited[0] = st.ncommit[0];
+      st.nwaited[1] = st.ncommit[1];
+    }
+    st.abort = __syncthreads_or(st.abort);
+    tc_fence_after();
+    if (!st.abort) {
+      const int warp = tid >> 5, lane = tid & 31;
+      const int quad = warp & 3, half = warp >> 2;
+      const int row = quad * 32 + lane;
+      const int cb = half * (NP / 2), ce = cb + NP / 2;
+      const int er = row < N ? s.expA[row] : 0;
+      for (int c0 = cb; c0 < ce; c0 += 8) {
+        uint32_t v0[8], v1[8], v2[8], v3[8];
+        const uint32_t ta = st.tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
+        tmem_ld8(ta, v0);
+        tmem_ld8(ta + (uint32_t)NP, v1);
+        tmem_ld8(ta + (uint32_t)(2 * NP), v2);
+        tmem_ld8(ta + (uint32_t)(3 * NP), v3);
+        tmem_wait_ld();
+        if (row < N) {
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const int j = c0 + jj;
+            if (j >= N) break;
+            const long long S = f2ll_int(v0[jj]) + f2ll_int(v1[jj]) + f2ll_int(v2[jj]) +
+                                f2ll_int(v3[jj]);
+            const double val = assemble(S, er + s.expB[j] - 1070);
+            const size_t idx = (size_t)row + (size_t)j * N;
+            double* o0 = reinterpret_cast<double*>(out0 + idx) + pass;
+            if (EPI == OZ_STORE) {
+              *o0 = val;
+            } else if (EPI == OZ_ADD2) {
+              *o0 += val;
+              double* o1 = reinterpret_cast<double*>(out1 + idx) + pass;
+              *o1 += val;
+            } else if (EPI == OZ_STORE_NORM) {
+              *o0 = val;
+              if (pass == 1) {
+                const float re = fabsf(d2f_bits(out0[idx].x)), im = fabsf(d2f_bits(val));
+                const float hi = fmaxf(re, im), lo = fminf(re, im);
+                if (hi > 0.f) {
+                  const float r = lo / hi;
+                  nrm += hi * sqrtf(fmaf(r, r, 1.f));
+                }
+              }
+            } else if (EPI == OZ_IMINUS) {
+              double v = -val;
+              if (pass == 0 && row == j) v += 1.0;
+              *o0 = v;
+            } else {   // OZ_ADDTO
+              *o0 = reinterpret_cast<const double*>(src + idx)[pass] + val;
+            }
+          }
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  return nrm;
+}
+
+__device__ float block_sum_f(float v, MxShared& s) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if (lane == 0) s.red[warp] = v;
+  __syncthreads();
+  float t = 0.f;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) t += s.red[w];
+    s.red[0] = t;
+  }
+  __syncthreads();
+  t = s.red[0];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ long long cabs1_key_f(float2 v) {
+  return (long long)__float_as_uint(fabsf(v.x) + fabsf(v.y));
+}
+
+// M = w I - X (FP64, kept in Mi for the refinement), then FP32 Gauss-Jordan
+// into G (FP64).  Returns 1 on an exact zero pivot (G = identity then).
+__device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, double2* Mi,
+                          double2* G, MxShared& s) {
+  const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
+  const int warp = tid >> 5, lane = tid & 31;
+  float2* sM = s.gj;
+  for (int e = tid; e < NN; e += T) {
+    const double2 x = X[e];
+    double2 m = make_double2(-x.x, -x.y);
+    if (e % (N + 1) == 0) m = make_double2(w.x - x.x, w.y - x.y);
+    Mi[e] = m;
+    sM[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+  }
+  if (tid == 0) s.misc[1] = 0;
+  __syncthreads();
+  for (int k = 0; k < N; ++k) {
+    if (warp == 0) {
+      long long best = -1;
+      int bi = N;
+      for (int i = k + lane; i < N; i += 32) {
+        const long long v = cabs1_key_f(sM[i + k * N]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      const int p = bi;
+      for (int i = lane; i < N; i += 32) s.colbuf[i] = sM[(i == p ? k : i) + k * N];
+      if (lane == 0) {
+        s.perm[k] = p;
+        if (best == 0) {
+          s.misc[1] = 1;
+        } else {
+          const float2 pv = sM[p + k * N];
+          const float inv_d = 1.0f / (pv.x * pv.x + pv.y * pv.y);
+          s.recip[0] = make_float2(pv.x * inv_d, -pv.y * inv_d);
+        }
+      }
+    }
+    __syncthreads();
+    if (s.misc[1]) break;
+    const int p = s.perm[k];
+    const float2 r = s.recip[0];
+    for (int j = tid; j < N; j += T) {
+      const float2 akj = sM[k + j * N];
+      const float2 apj = sM[p + j * N];
+      if (p != k) sM[p + j * N] = akj;
+      const float2 nk = (j == k) ? r
+                                 : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
+                                               fmaf(apj.x, r.y, apj.y * r.x));
+      sM[k + j * N] = nk;
+      s.rowbuf[j] = nk;
+    }
+    __syncthreads();
+    for (int e = tid; e < NN; e += T) {
+      const int i = e % N, j = e / N;
+      if (i != k) {
+        float2 v = (j == k) ? make_float2(0.f, 0.f) : sM[e];
+        const float2 f = s.colbuf[i];
+        const float2 rk = s.rowbuf[j];
+        v.x = fmaf(-f.x, rk.x, v.x);
+        v.x = fmaf(f.y, rk.y, v.x);
+        v.y = fmaf(-f.x, rk.y, v.y);
+        v.y = fmaf(-f.y, rk.x, v.y);
+        sM[e] = v;
+      }
+    }
+    __syncthreads();
+  }
+  const int singular = s.misc[1];
+  if (tid == 0) {
+    for (int j = 0; j < N; ++j) s.cols[j] = j;
+    if (!singular) {
+      for (int k = N - 1; k >= 0; --k) {
+        const int p = s.perm[k];
+        const int t = s.cols[k];
+        s.cols[k] = s.cols[p];
+        s.cols[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < NN; e += T) {
+    const int i = e % N, j = e / N;
+    if (singular) {
+      G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    } else {
+      const float2 v = sM[i + s.cols[j] * N];
+      G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
+    }
+  }
+  __syncthreads();
+  return singular;
+}
+
+// (w I - X)^-1 into *Gp: FP32 Gauss-Jordan + ns Newton-Schulz steps on the
+// split tensor-core products.  Uses Mi, R, Gn as work; swaps *Gp and *Gn.
+__device__ int mixed_inverse(const double2* X, double2 w, int N, int NP, int ns, double2** Gp,
+                             double2** Gnp, double2* Mi, double2* R, MxShared& s, MxState& st) {
+  const int sing = gj32_start(X, w, N, Mi, *Gp, s);
+  for (int t = 0; t < ns && !st.abort; ++t) {
+    oz_gemm<OZ_IMINUS>(Mi, *Gp, N, NP, R, nullptr, nullptr, s, st);      // R = I - M G
+    oz_gemm<OZ_ADDTO>(*Gp, R, N, NP, *Gnp, nullptr, *Gp, s, st);         // Gn = G + G R
+    double2* tmp = *Gp;
+    *Gp = *Gnp;
+    *Gnp = tmp;
+  }
+  return sing;
+}
+
+__global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, int ns_iter,
+                                                            int ns_final) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
+  const int NP = (N + 15) & ~15;
+  const int bufbytes = 2 * NSL * APLANE + 2 * NSL * NP * KCH * 2;
+  MxShared s;
+  s.buf[0] = smraw;
+  s.buf[1] = smraw + bufbytes;
+  s.gj = reinterpret_cast<float2*>(smraw);
+  unsigned char* tail = smraw + 2 * bufbytes;
+  s.colbuf = reinterpret_cast<float2*>(tail);
+  s.rowbuf = s.colbuf + 128;
+  s.recip = s.rowbuf + 128;
+  s.perm = reinterpret_cast<int*>(s.recip + 2);
+  s.cols = s.perm + 128;
+  s.expA = s.cols + 128;
+  s.expB = s.expA + 128;
+  s.red = reinterpret_cast<float*>(s.expB + 128);
+  s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
+  s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
+  s.misc = reinterpret_cast<int*>(s.tslot + 2);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if ((tid >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(s.tslot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  MxState st;
+  st.tmem = *s.tslot;
+  st.ncommit[0] = st.ncommit[1] = 0;
+  st.nwaited[0] = st.nwaited[1] = 0;
+  st.abort = 0;
+
+  double2* W = a.ws + (size_t)blockIdx.x * 11 * NN;
+  double2* E = W;
+  double2* ES = W + (size_t)NN;
+  double2* ET = W + (size_t)2 * NN;
+  double2* Al = W + (size_t)3 * NN;
+  double2* Be = W + (size_t)4 * NN;
+  double2* G = W + (size_t)5 * NN;
+  double2* M1 = W + (size_t)6 * NN;
+  double2* M2 = W + (size_t)7 * NN;
+  double2* Mi = W + (size_t)8 * NN;
+  double2* R = W + (size_t)9 * NN;
+  double2* Gn = W + (size_t)10 * NN;
+
+  for (;;) {
+    if (tid == 0) s.misc[0] = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int inst = s.misc[0];
+    __syncthreads();
+    if (inst >= a.n_inst || st.abort) break;
+    const int ik = inst / a.nomega, iw = inst % a.nomega;
+    const double2* H00 = a.h + (size_t)ik * 2 * NN;
+    const double2* H01 = H00 + NN;
+    const double2 w = make_double2(a.omega[iw], a.eta);
+    for (int e = tid; e < NN; e += T) {
+      const double2 h = H00[e];
+      E[e] = h;
+      ES[e] = h;
+      ET[e] = h;
+      Al[e] = H01[e];
+      const int i = e % N, j = e / N;
+      const double2 t = H01[j + (size_t)i * N];
+      Be[e] = make_double2(t.x, -t.y);
+    }
+    __syncthreads();
+    int stat = 0, it = 0;
+    bool conv = false;
+    for (int itc = 1; itc <= a.itermax && !st.abort; ++itc) {
+      it = itc;
+      if (mixed_inverse(E, w, N, NP, ns_iter, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+      oz_gemm<OZ_STORE>(Al, G, N, NP, M1, nullptr, nullptr, s, st);
+      oz_gemm<OZ_STORE>(Be, G, N, NP, M2, nullptr, nullptr, s, st);
+      oz_gemm<OZ_ADD2>(M1, Be, N, NP, E, ES, nullptr, s, st);
+      oz_gemm<OZ_ADD2>(M2, Al, N, NP, E, ET, nullptr, s, st);
+      const float part = oz_gemm<OZ_STORE_NORM>(M1, Al, N, NP, Gn, nullptr, nullptr, s, st);
+      oz_gemm<OZ_STORE>(M2, Be, N, NP, R, nullptr, nullptr, s, st);
+      double2* t0 = Al;
+      Al = Gn;
+      Gn = t0;
+      double2* t1 = Be;
+      Be = R;
+      R = t1;
+      const float nrm = block_sum_f(part, s);
+      if ((double)nrm <= a.tol) {
+        conv = true;
+        break;
+      }
+    }
+    if (!conv) stat |= PT_NOT_CONVERGED;
+    const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
+    double dl = 0.0, dr = 0.0, db = 0.0;
+    if (mixed_inverse(ES, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    if (a.gll)
+      for (int e = tid; e < NN; e += T) a.gll[(size_t)inst * NN + e] = G[e];
+    if (tid == 0)
+      for (int q = 0; q < a.ntop; ++q) {
+        const int io = a.top[q] - 1;
+        const double v = G[io + (size_t)io * N].y;
+        dl = a.divide_by_pi ? dl - v / PI_REF : dl - v;
+      }
+    __syncthreads();
+    if (mixed_inverse(ET, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    if (a.grr)
+      for (int e = tid; e < NN; e += T) a.grr[(size_t)inst * NN + e] = G[e];
+    if (tid == 0)
+      for (int q = 0; q < a.nbot; ++q) {
+        const int io = N - a.nw + a.bot[q] - 1;
+        const double v = G[io + (size_t)io * N].y;
+        dr = a.divide_by_pi ? dr - v / PI_REF : dr - v;
+      }
+    __syncthreads();
+    if (mixed_inverse(E, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    if (a.gb)
+      for (int e = tid; e < NN; e += T) a.gb[(size_t)inst * NN + e] = G[e];
+    if (tid == 0) {
+      for (int i = 0; i < N; ++i) {
+        const double v = G[i + (size_t)i * N].y;
+        db = a.divide_by_pi ? db - v / PI_REF : db - v;
+      }
+      if (st.abort) stat |= PT_TIMEOUT;
+      if (!isfinite(dl) || !isfinite(dr) || !isfinite(db)) stat |= PT_NONFINITE;
+      a.dos_l[oidx] = dl;
+      a.dos_r[oidx] = dr;
+      a.dos_bulk[oidx] = db;
+      if (a.iters) a.iters[oidx] = it;
+      if (a.status) a.status[oidx] = (uint8_t)stat;
+    }
+    __syncthreads();
+  }
+  // drain: every committed MMA must finish before tensor memory is released
+  for (int b = 0; b < 2; ++b)
+    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if ((tid >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(512));
+}
+
+// single complex product / inverse through the same device code (one CTA)
+__global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const double2* X,
+                                                        const double2* Y, double2* C, double2* ws,
+                                                        int ns, int* status) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  const int NP = (N + 15) & ~15;
+  const int NN = N * N;
+  const int bufbytes = 2 * NSL * APLANE + 2 * NSL * NP * KCH * 2;
+  MxShared s;
+  s.buf[0] = smraw;
+  s.buf[1] = smraw + bufbytes;
+  s.gj = reinterpret_cast<float2*>(smraw);
+  unsigned char* tail = smraw + 2 * bufbytes;
+  s.colbuf = reinterpret_cast<float2*>(tail);
+  s.rowbuf = s.colbuf + 128;
+  s.recip = s.rowbuf + 128;
+  s.perm = reinterpret_cast<int*>(s.recip + 2);
+  s.cols = s.perm + 128;
+  s.expA = s.cols + 128;
+  s.expB = s.expA + 128;
+  s.red = reinterpret_cast<float*>(s.expB + 128);
+  s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
+  s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
+  s.misc = reinterpret_cast<int*>(s.tslot + 2);
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if ((tid >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(s.tslot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  MxState st;
+  st.tmem = *s.tslot;
+  st.ncommit[0] = st.ncommit[1] = 0;
+  st.nwaited[0] = st.nwaited[1] = 0;
+  st.abort = 0;
+  int sing = 0;
+  if (op == 0) {
+    oz_gemm<OZ_STORE>(X, Y, N, NP, C, nullptr, nullptr, s, st);
+  } else {
+    // C = X^-1: X given directly, so pass -X with w = 0 (M = 0*I - (-X) = X)
+    double2* negX = ws + 4 * (size_t)NN;
+    for (int e = tid; e < NN; e += blockDim.x) negX[e] = make_double2(-X[e].x, -X[e].y);
+    __syncthreads();
+    double2* G = ws;
+    double2* Gn = ws + NN;
+    sing = mixed_inverse(negX, make_double2(0.0, 0.0), N, NP, ns, &G, &Gn, ws + 2 * (size_t)NN,
+                         ws + 3 * (size_t)NN, s, st);
+    for (int e = tid; e < NN; e += blockDim.x) C[e] = G[e];
+  }
+  for (int b = 0; b < 2; ++b)
+    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid == 0) *status = (st.abort ? PT_TIMEOUT : 0) | (sing ? PT_SINGULAR : 0);
+  if ((tid >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(512));
+}
+
+size_t mixed_smem(int N) {
+  const int NP = (N + 15) & ~15;
+  const size_t bufbytes = 2 * NSL * APLANE + 2 * NSL * (size_t)NP * KCH * 2;
+  size_t planes = 2 * bufbytes;
+  const size_t gj = (size_t)N * N * sizeof(float2);
+  if (gj > planes) planes = gj;
+  return planes + 128 * 8 * 2 + 16 + 128 * 4 * 4 + 32 * 4 + 16 + 8 + 16;
+}
+
+}  // namespace
+
+int decim_mixed_max_n() { return 128; }
+
+size_t decim_mixed_ws_matrices() { return 11; }
+
+cudaError_t decim_mixed_config(int N, DecimConfig* cfg) {
+  cfg->threads = MX_T;
+  cfg->KC = 0;
+  cfg->RP = 0;
+  // at least 116 KB so that two CTAs never share an SM (each allocates all 512 TMEM columns)
+  cfg->smem = mixed_smem(N) > (size_t)(116 << 10) ? mixed_smem(N) : (size_t)(116 << 10);
+  cudaError_t e = cudaFuncSetAttribute(k_decimate_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)cfg->smem);
+  if (e != cudaSuccess) return e;
+  int occ = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_decimate_mixed, MX_T, cfg->smem);
+  if (e != cudaSuccess) return e;
+  cfg->ctas_per_sm = occ > 1 ? 1 : occ;     // tensor memory is allocated whole (512 columns)
+  return cudaSuccess;
+}
+
+cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
+                                  cudaStream_t s) {
+  k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 2, 3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_unit(int op, int N, const double2* X, const double2* Y, double2* C,
+                              double2* ws, int ns, int* status, cudaStream_t s) {
+  const size_t smem = mixed_smem(N) > (size_t)(116 << 10) ? mixed_smem(N) : (size_t)(116 << 10);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_mixed_unit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_mixed_unit<<<1, MX_T, smem, s>>>(op, N, X, Y, C, ws, ns, status);
+  return cudaGetLastError();
+}
+
+}  // namespace wtg
