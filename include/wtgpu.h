@@ -153,6 +153,25 @@ int wtg_surface_spectrum(wtg_model_t model, int nk, const double* k,
                          int32_t* iters, uint8_t* status);
 
 /*
+ * wtg_surface_spectrum plus the spin-resolved surface spectra
+ * sx/sy/sz_l = -sum Im (GLL sigma_{x,y,z})(io,io) and sx/sy/sz_r from GRR, with
+ * the Pauli matrices of src/surfstat.f90:103-114 (|up..up down..down> basis
+ * per Num_wann block).  Only the entries of G that sigma*G needs are read,
+ * replacing the six full products of the reference.
+ *   arc_mode 0: surfstat (src/surfstat.f90:162-192): no 1/pi, and the right
+ *               spin sums run over the TOP orbital list (as the reference does);
+ *   arc_mode 1: SurfaceDOSkk spin texture (src/fermiarc.f90:250-330): every
+ *               term divided by pi, right sums over Ndim - nw + bottom orbitals.
+ *   spin_out   double[6 * nk * nomega]: sx_l, sy_l, sz_l, sx_r, sy_r, sz_r, each
+ *              (nk, nomega) column-major, host buffer.
+ */
+int wtg_surface_spectrum_spin(wtg_model_t model, int nk, const double* k, int nomega,
+                              const double* omega, double eta, double tol, int itermax,
+                              int ntop, const int* top, int nbot, const int* bot, int arc_mode,
+                              int precision, double* dos_l, double* dos_r, double* dos_bulk,
+                              double* spin_out, int32_t* iters, uint8_t* status);
+
+/*
  * Same computation with every array already on the device, enqueued on
  * `stream` (a cudaStream_t, NULL = legacy default stream) without a host
  * synchronisation.  top/bot are host arrays (they are small and copied

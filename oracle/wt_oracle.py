@@ -201,20 +201,30 @@ def spin_matrices(nw, np_):
     return sx, sy, sz
 
 
-def spin_sums(gll, grr, top, nw, np_):
-    """Spin-resolved sums, src/surfstat.f90:162-192.
+def spin_sums(gll, grr, top, nw, np_, bot=None, divide_by_pi=False):
+    """Spin-resolved sums with six full products G*sigma, as the reference does.
 
-    Six full products G*sigma as the reference does; note the reference uses
-    TopOrbitals for the right surface too (src/surfstat.f90:178-192).
+    surfstat (bot=None, src/surfstat.f90:162-192): the right surface also runs
+    over TopOrbitals (src/surfstat.f90:178-192), no 1/pi.
+    SurfaceDOSkk spin texture (bot given, divide_by_pi, src/fermiarc.f90:272-327):
+    the right surface runs over Ndim - Num_wann + BottomOrbitals, each term / pi.
     Returns (sx_l, sy_l, sz_l, sx_r, sy_r, sz_r)."""
     sx, sy, sz = spin_matrices(nw, np_)
+    n = gll.shape[0]
     out = []
-    for g in (gll, grr):
+    for side, g in enumerate((gll, grr)):
+        if side == 1 and bot is not None:
+            idx = [n - nw + io for io in bot]
+        else:
+            idx = list(top)
         for s in (sx, sy, sz):
             c = mat_mul(g, s)
             acc = 0.0
-            for io in top:
-                acc = acc - c[io - 1, io - 1].imag
+            for io in idx:
+                if divide_by_pi:
+                    acc = acc - c[io - 1, io - 1].imag / PI_REF
+                else:
+                    acc = acc - c[io - 1, io - 1].imag
             out.append(acc)
     return tuple(out)
 
@@ -276,7 +286,8 @@ def surface_spectrum(hmnr, irvec, ndegen, nw, np_, kpts, omegas, eta, top, bot,
             out["iters"][ik, j] = it
             out["status"][ik, j] = st
             if with_spin:
-                s = spin_sums(gll, grr, top, nw, np_)
+                s = spin_sums(gll, grr, top, nw, np_, bot=(bot if scale != 1.0 else None),
+                              divide_by_pi=(scale != 1.0))
                 for name, v in zip(("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r"), s):
                     out[name][ik, j] = v
     return out

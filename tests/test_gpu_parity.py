@@ -194,3 +194,23 @@ def test_many_points_properties(lib):
     assert (full["dos_bulk"] > 0).all() and (full["dos_l"] > 0).all()
     for name in ("dos_l", "dos_r", "dos_bulk"):
         assert np.array_equal(full[name][10:13, 5:9], part[name])
+
+
+@pytest.mark.parametrize("nw,np_,arc", [(6, 2, False), (6, 2, True), (5, 1, False), (10, 3, True)])
+def test_spin_resolved_spectra(lib, nw, np_, arc):
+    """sx/sy/sz of GLL and GRR (src/surfstat.f90:162-192, src/fermiarc.f90:250-330)
+    against the oracle's six full products with the Pauli matrices."""
+    m = synthetic.make_model(nw, np_, seed=50 + nw)
+    kp = synthetic.random_kpoints(2, seed=nw)
+    om = np.array([-0.2, 0.35]) * EV
+    top = [1, 2, nw]
+    bot = [1, (nw + 1) // 2]
+    ref = O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, nw, np_, kp, om, 1e-2 * EV, top, bot,
+                             scale=(1.0 / O.PI_REF if arc else 1.0), with_spin=True)
+    with api.Model.from_surface_model(m) as g:
+        got = g.surface_spectrum_spin(kp, om, 1e-2 * EV, top, bot, arc=arc)
+    for name in ("dos_l", "dos_r", "dos_bulk"):
+        assert rel(got[name], ref[name]) <= RTOL, name
+    for name in ("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r"):
+        scale = np.abs(ref["dos_l"]).max()
+        assert np.max(np.abs(got[name] - ref[name])) <= 1e-9 * scale, name

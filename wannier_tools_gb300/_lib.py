@@ -47,6 +47,9 @@ SIGNATURES = {
                                                _vp, _vp, _vp, _vp, _vp, _vp]),
     "wtg_mat_mul": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int]),
     "wtg_inv": (C.c_int, [C.c_int, _dp, C.c_int, _ip]),
+    "wtg_surface_spectrum_spin": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, C.c_double, C.c_double,
+                                             C.c_int, C.c_int, _ip, C.c_int, _ip, C.c_int, C.c_int,
+                                             _dp, _dp, _dp, _dp, _i32p, _u8p]),
     "wtg_model_profile": (C.c_int, [_vp, C.c_int]),
     "wtg_model_profile_read": (C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_longlong), _ip]),
     "wtg_probe_fp64_peak": (C.c_int, [_dp]),

@@ -144,6 +144,36 @@ class Model:
         res["status"] = status.reshape((nk, nwo), order="F")
         return res
 
+    # -- spin-resolved spectrum (host buffers) ------------------------------
+    def surface_spectrum_spin(self, kpts, omegas, eta: float, top, bot, arc: bool = False,
+                              tol: float = ACCURACY_REF, itermax: int = ITERMAX_REF,
+                              precision: int = PREC_FP64) -> dict:
+        """surface_spectrum plus sx_l, sy_l, sz_l, sx_r, sy_r, sz_r ((nk, nomega)
+        arrays): surfstat's spin sums (arc=False, src/surfstat.f90:162-192) or
+        SurfaceDOSkk's spin texture (arc=True, src/fermiarc.f90:250-330)."""
+        kp = np.asarray(kpts, dtype=np.float64).reshape(-1, 2)
+        kcol = np.ascontiguousarray(kp.T)
+        nk = kcol.shape[1]
+        w = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64).ravel())
+        nwo = w.shape[0]
+        top_a = np.ascontiguousarray(np.asarray(top, dtype=np.int32).ravel())
+        bot_a = np.ascontiguousarray(np.asarray(bot, dtype=np.int32).ravel())
+        outs = {name: np.zeros(nk * nwo) for name in ("dos_l", "dos_r", "dos_bulk")}
+        spin = np.zeros(6 * nk * nwo)
+        iters = np.zeros(nk * nwo, np.int32)
+        status = np.zeros(nk * nwo, np.uint8)
+        check(_lib.load().wtg_surface_spectrum_spin(
+            self._handle, nk, _dptr(kcol), nwo, _dptr(w), float(eta), float(tol), int(itermax),
+            len(top_a), _iptr(top_a), len(bot_a), _iptr(bot_a), int(bool(arc)), precision,
+            _dptr(outs["dos_l"]), _dptr(outs["dos_r"]), _dptr(outs["dos_bulk"]), _dptr(spin),
+            iters.ctypes.data_as(C.POINTER(C.c_int32)), status.ctypes.data_as(C.POINTER(C.c_uint8))))
+        res = {name: v.reshape((nk, nwo), order="F") for name, v in outs.items()}
+        for c, name in enumerate(("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r")):
+            res[name] = spin[c * nk * nwo:(c + 1) * nk * nwo].reshape((nk, nwo), order="F")
+        res["iters"] = iters.reshape((nk, nwo), order="F")
+        res["status"] = status.reshape((nk, nwo), order="F")
+        return res
+
     # -- batched spectrum (device buffers, asynchronous) --------------------
     def surface_spectrum_device(self, d_k, d_omega, eta: float, top, bot, d_dos_l, d_dos_r,
                                 d_dos_bulk, d_iters=None, d_status=None,

@@ -99,7 +99,8 @@ namespace {
 int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const double* d_omega,
                  double eta, double tol, int itermax, int ntop, const int* top, int nbot,
                  const int* bot, int divide_by_pi, int precision, double* d_dl, double* d_dr,
-                 double* d_db, int32_t* d_it, uint8_t* d_st, cudaStream_t s) {
+                 double* d_db, int32_t* d_it, uint8_t* d_st, cudaStream_t s,
+                 double* const* d_spin = nullptr, int spin_right_bottom = 0) {
   const int N = m->N;
   const bool mixed = precision == WTG_PREC_MIXED;
   const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_max_n();
@@ -155,6 +156,9 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
   a.nbot = nbot;
   for (int q = 0; q < ntop; ++q) a.top[q] = top[q];
   for (int q = 0; q < nbot; ++q) a.bot[q] = bot[q];
+  if (d_spin)
+    for (int c = 0; c < 6; ++c) a.spin[c] = d_spin[c];
+  a.spin_right_bottom = spin_right_bottom;
   int chunk_id = 0;
   for (int k0 = 0; k0 < nk; k0 += kchunk, ++chunk_id) {
     const int kc = std::min(kchunk, nk - k0);
@@ -526,7 +530,7 @@ static int unit_op(int op, int n, const double* a, const double* b, double* c, i
   cudaError_t e = cudaMemcpy(dx, a, sizeof(double2) * nn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && op == 0) e = cudaMemcpy(dy, b, sizeof(double2) * nn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = mixed ? wtg::launch_mixed_unit(op, n, dx, dy, dc, dws, 3, dst, 0)
+    e = mixed ? wtg::launch_mixed_unit(op, n, dx, dy, dc, dws, 8, dst, 0)
               : wtg::launch_fp64_unit(op, n, dx, dy, dc, dws, dst, 0);
   if (e == cudaSuccess) e = cudaMemcpy(c, dc, sizeof(double2) * nn, cudaMemcpyDeviceToHost);
   int st = 0;
@@ -579,6 +583,57 @@ int wtg_model_profile_read(wtg_model_t m, double* fourier_ms, double* decim_ms,
   if (launches) *launches = m->launches;
   if (decim_launches) *decim_launches = (int)m->decim_ev.size();
   return WTG_OK;
+}
+
+int wtg_surface_spectrum_spin(wtg_model_t m, int nk, const double* k, int nomega,
+                              const double* omega, double eta, double tol, int itermax, int ntop,
+                              const int* top, int nbot, const int* bot, int arc_mode,
+                              int precision, double* dos_l, double* dos_r, double* dos_bulk,
+                              double* spin_out, int32_t* iters, uint8_t* status) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  if (nk < 0 || nomega < 0 || itermax < 0) return fail(WTG_EINVAL, "negative size");
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
+  if (nk == 0 || nomega == 0) return WTG_OK;
+  if (!k || !omega || !dos_l || !dos_r || !dos_bulk || !spin_out)
+    return fail(WTG_EINVAL, "null array");
+  int rc = check_lists(m->nw, ntop, top, nbot, bot);
+  if (rc != WTG_OK) return rc;
+  std::lock_guard<std::mutex> lk(m->mu);
+  WTG_CK(cudaSetDevice(m->device));
+  const size_t npts = (size_t)nk * nomega;
+  cudaStream_t s = m->stream;
+  WTG_CK(cudaStreamWaitEvent(s, m->done, 0));
+  WTG_CK(m->k_in.ensure(sizeof(double) * 2 * (size_t)nk));
+  WTG_CK(m->w_in.ensure(sizeof(double) * (size_t)nomega));
+  WTG_CK(m->out_dos.ensure(sizeof(double) * 9 * npts));
+  WTG_CK(m->out_it.ensure(sizeof(int32_t) * npts));
+  WTG_CK(m->out_st.ensure(sizeof(uint8_t) * npts));
+  WTG_CK(cudaMemcpyAsync(m->k_in.p, k, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice, s));
+  WTG_CK(cudaMemcpyAsync(m->w_in.p, omega, sizeof(double) * nomega, cudaMemcpyHostToDevice, s));
+  double* dd = (double*)m->out_dos.p;
+  double* dspin[6];
+  for (int c = 0; c < 6; ++c) dspin[c] = dd + (3 + c) * npts;
+  rc = run_spectrum(m, nk, (const double*)m->k_in.p, nomega, (const double*)m->w_in.p, eta, tol,
+                    itermax, ntop, top, nbot, bot, arc_mode ? 1 : 0, precision, dd, dd + npts,
+                    dd + 2 * npts, (int32_t*)m->out_it.p, (uint8_t*)m->out_st.p, s, dspin,
+                    arc_mode ? 1 : 0);
+  if (rc != WTG_OK) return rc;
+  WTG_CK(cudaMemcpyAsync(dos_l, dd, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(dos_r, dd + npts, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(dos_bulk, dd + 2 * npts, sizeof(double) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(spin_out, dd + 3 * npts, sizeof(double) * 6 * npts, cudaMemcpyDeviceToHost, s));
+  std::vector<uint8_t> st_local;
+  uint8_t* st_host = status;
+  if (!st_host) {
+    st_local.resize(npts);
+    st_host = st_local.data();
+  }
+  WTG_CK(cudaMemcpyAsync(st_host, m->out_st.p, npts, cudaMemcpyDeviceToHost, s));
+  if (iters)
+    WTG_CK(cudaMemcpyAsync(iters, m->out_it.p, sizeof(int32_t) * npts, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  return count_flagged(st_host, npts);
 }
 
 int wtg_last_error(char* buf, int len) {

@@ -18,6 +18,46 @@ constexpr int PT_SINGULAR = 2;
 constexpr int PT_NONFINITE = 4;
 constexpr int PT_TIMEOUT_BIT = 8;
 
+// Spin-resolved sums -Im (G sigma_a)(io, io) over an orbital list, with the
+// Pauli matrices of src/surfstat.f90:103-114 (|up..up down..down> basis per
+// Num_wann block): (G sx)(io,io) = G(io,p), (G sy)(io,io) = +-i G(io,p),
+// (G sz)(io,io) = +-G(io,io), p the spin partner of io.  `g(i, j)` returns G.
+template <class GetG>
+__device__ void spin_sums(GetG g, int nw, int n_list, const int* list, int offset,
+                          int divide_by_pi, double& sx, double& sy, double& sz) {
+  const int nwh = nw / 2;
+  for (int q = 0; q < n_list; ++q) {
+    const int io = offset + list[q] - 1;
+    const int jl = io % nw;
+    int partner = -1;
+    double sgn = 0.0;
+    if (jl < nwh) {
+      partner = io + nwh;
+      sgn = 1.0;
+    } else if (jl < 2 * nwh) {
+      partner = io - nwh;
+      sgn = -1.0;
+    }
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    if (partner >= 0) {
+      const double2 gp = g(io, partner);
+      const double2 gd = g(io, io);
+      vx = gp.y;
+      vy = sgn * gp.x;
+      vz = sgn * gd.y;
+    }
+    if (divide_by_pi) {
+      sx = sx - vx / PI_REF;
+      sy = sy - vy / PI_REF;
+      sz = sz - vz / PI_REF;
+    } else {
+      sx = sx - vx;
+      sy = sy - vy;
+      sz = sz - vz;
+    }
+  }
+}
+
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
@@ -65,6 +105,8 @@ struct DecimArgs {
   double* dos_bulk;
   int32_t* iters;             // may be null
   uint8_t* status;            // may be null
+  double* spin[6];            // optional sx_l, sy_l, sz_l, sx_r, sy_r, sz_r (null = skip)
+  int spin_right_bottom;      // 0: right spin over the top list (surfstat), 1: over Ndim-nw+bottom
   double2* gll;               // optional full outputs [n_inst][N*N] (null = skip)
   double2* grr;
   double2* gb;

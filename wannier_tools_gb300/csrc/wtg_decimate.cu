@@ -114,12 +114,16 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
     // GLL = (w - eps_s)^-1                                   // :127-128
     if (gj_invert(ES, w, N, s)) st |= PT_SINGULAR;
     if (a.gll) gj_store(N, s, a.gll + (size_t)inst * NN);
+    double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (tid == 0) {
       for (int q = 0; q < a.ntop; ++q) {
         const int io = a.top[q] - 1;
         const double v = gj_diag(N, s, io).y;
         dl = a.divide_by_pi ? dl - v / PI_REF : dl - v;
       }
+      if (a.spin[0])                                          // src/surfstat.f90:162-177
+        spin_sums([&](int i, int j) { return s.big[i + s.cols[j] * N]; }, a.nw, a.ntop, a.top, 0,
+                  a.divide_by_pi, spin[0], spin[1], spin[2]);
     }
     __syncthreads();
     // GRR = (w - eps_t)^-1                                   // :130-131
@@ -130,6 +134,13 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
         const int io = N - a.nw + a.bot[q] - 1;
         const double v = gj_diag(N, s, io).y;
         dr = a.divide_by_pi ? dr - v / PI_REF : dr - v;
+      }
+      if (a.spin[0]) {                                        // src/surfstat.f90:178-192
+        auto gr = [&](int i, int j) { return s.big[i + s.cols[j] * N]; };
+        if (a.spin_right_bottom)                              // src/fermiarc.f90:300-327
+          spin_sums(gr, a.nw, a.nbot, a.bot, N - a.nw, a.divide_by_pi, spin[3], spin[4], spin[5]);
+        else
+          spin_sums(gr, a.nw, a.ntop, a.top, 0, a.divide_by_pi, spin[3], spin[4], spin[5]);
       }
     }
     __syncthreads();
@@ -145,6 +156,8 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
       a.dos_l[oidx] = dl;
       a.dos_r[oidx] = dr;
       a.dos_bulk[oidx] = db;
+      if (a.spin[0])
+        for (int c = 0; c < 6; ++c) a.spin[c][oidx] = spin[c];
       if (a.iters) a.iters[oidx] = it;
       if (a.status) a.status[oidx] = (uint8_t)st;
     }

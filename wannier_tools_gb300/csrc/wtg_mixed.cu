@@ -2,20 +2,25 @@
 //
 // Every complex product of surfgreen_1985 (src/surfgreen.f90:92-116, zgemm at
 // src/mat_mul.f90:23) runs as an exactly-split BF16 product on tcgen05:
-//   * each FP64 operand is written as 42-bit fixed point against a shared
+//   * each FP64 operand is written as 49-bit fixed point against a shared
 //     exponent per row (left factor) or per column (right factor) and cut into
-//     six 7-bit digits; a digit is an exact BF16 value (with a power-of-two
+//     seven 7-bit digits; a digit is an exact BF16 value (with a power-of-two
 //     scale folded in);
-//   * slice products A^p B^q with p + q <= 7 are issued as BF16 MMAs with FP32
+//   * slice products A^p B^q with p + q <= 8 are issued as BF16 MMAs with FP32
 //     accumulators in tensor memory, one accumulator per slice order
-//     t = p + q for t = 2, 3, 4 (sums of at most 3 * 2K digit products stay
-//     below 2^24, so these accumulations are exact) and one for t >= 5 (rounded
-//     at 2^-45 of the result);
+//     t = p + q for t = 2, 3, 4, 5 (sums of at most 4 * 2K digit products stay
+//     below 2^24, where the tensor core's accumulation is exact) and one for
+//     t >= 6 (its accumulation truncates; at 2^-28 of the result that costs
+//     ~2^-44);  49 bits are needed because the Newton-Schulz refinement below
+//     can only be as accurate as its residual product;
 //   * the four accumulators are read back (tcgen05.ld), converted to integers
 //     and summed in int64, and the FP64 result is assembled with integer
 //     operations (no FP64 arithmetic for the product itself).
-// The complex product is two passes: Cr = Xr Yr - Xi Yi (the second term via
-// the instruction's negate-B bit) and Ci = Xr Yi + Xi Yr.
+// The complex product runs in passes: Cr = Xr Yr - Xi Yi (the second term via
+// the instruction's negate-B bit) and Ci = Xr Yi + Xi Yr, each over all output
+// columns when five accumulators fit in the 512 tensor-memory columns
+// (Ndim <= 96) and over two column halves otherwise.  Digits become BF16 bits
+// through per-slice lookup tables in shared memory.
 // Inverses (zgesv with identity, src/inverse.f90:43-55) are a shared-memory
 // FP32 Gauss-Jordan followed by Newton-Schulz refinement X <- X + X (I - M X)
 // whose two products are the split products above, so the inverse reaches the
@@ -40,7 +45,7 @@ namespace {
 #include "wtg_fp64_dev.cuh"
 
 constexpr int MX_T = 256;            // threads per CTA (8 warps)
-constexpr int NSL = 6;               // digits per operand
+constexpr int NSL = 7;               // digits per operand (49-bit fixed point)
 constexpr int KCH = 16;              // K per staged chunk
 constexpr int APLANE = 128 * KCH * 2;  // bytes of one A plane (128 rows x 16 bf16)
 constexpr unsigned SPIN_LIMIT = 1u << 22;
@@ -117,15 +122,15 @@ __device__ __forceinline__ int bexp(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
-// |x| as 42-bit fixed point against biased exponent E (|x| < 2^(E-1022))
-__device__ __forceinline__ unsigned long long fixed42(double x, int E, unsigned& neg) {
+// |x| as 49-bit fixed point against biased exponent E (|x| < 2^(E-1022))
+__device__ __forceinline__ unsigned long long fixed49(double x, int E, unsigned& neg) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   neg = (unsigned)(u >> 63);
   int ex = (int)((u >> 52) & 0x7FF);
   unsigned long long m = u & 0xFFFFFFFFFFFFFull;
   if (ex) m |= 1ull << 52;
   else ex = 1;
-  const int sh = E - ex + 11;
+  const int sh = E - ex + 4;
   return sh < 64 ? (m >> sh) : 0ull;
 }
 
@@ -138,12 +143,13 @@ __device__ __forceinline__ uint32_t bf16_digit(uint32_t d, int s, uint32_t neg) 
   return (neg << 15) | (e << 7) | mant;
 }
 
-// integer value of an integer-valued float
+// integer value of an integer-valued float, divided by 2^7 (truncating):
+// keeps the int64 sum of the slice-order accumulators below 2^58
 __device__ __forceinline__ long long f2ll_int(uint32_t w) {
   const int e = (int)((w >> 23) & 0xFF);
-  if (e < 127) return 0;
+  if (e < 134) return 0;
   const long long m = (long long)((w & 0x7FFFFFu) | 0x800000u);
-  const int sh = e - 150;
+  const int sh = e - 157;
   const long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
   return (w >> 31) ? -v : v;
 }
@@ -186,7 +192,7 @@ __device__ __forceinline__ double f2d_bits(float f) {     // exact FP32 -> FP64
 // ---- shared state ------------------------------------------------------------
 
 struct MxShared {
-  unsigned char* buf[2];   // per buffer: 12 A planes then 12 B planes
+  unsigned char* buf[2];   // per buffer: 2*NSL A planes then 2*NSL B planes
   float2* gj;              // FP32 Gauss-Jordan matrix (aliases the buffers)
   float2* colbuf;
   float2* rowbuf;
@@ -199,7 +205,40 @@ struct MxShared {
   uint64_t* mbar;          // [2]
   uint32_t* tslot;
   int* misc;               // 0 instance, 1 singular, 2 abort
+  uint16_t* lutA;          // [NSL][128] BF16 bits of d * 2^(7(3-p))
+  uint16_t* lutB;          // [NSL][128] BF16 bits of d * 2^(7(5-q))
 };
+
+constexpr int NACC = 5;              // accumulators per pass: t = 2, 3, 4, 5 exact; t >= 6
+
+__device__ __forceinline__ int bufbytes_of(int NP) {
+  return 2 * NSL * APLANE + 2 * NSL * NP * KCH * 2;
+}
+
+// shared-memory layout: two operand buffers (the FP32 Gauss-Jordan matrix
+// aliases them), then the small arrays
+__device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int NP) {
+  MxShared s;
+  const int bb = bufbytes_of(NP);
+  s.buf[0] = smraw;
+  s.buf[1] = smraw + bb;
+  s.gj = reinterpret_cast<float2*>(smraw);
+  unsigned char* tail = smraw + 2 * bb;
+  s.colbuf = reinterpret_cast<float2*>(tail);
+  s.rowbuf = s.colbuf + 128;
+  s.recip = s.rowbuf + 128;
+  s.perm = reinterpret_cast<int*>(s.recip + 2);
+  s.cols = s.perm + 128;
+  s.expA = s.cols + 128;
+  s.expB = s.expA + 128;
+  s.red = reinterpret_cast<float*>(s.expB + 128);
+  s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
+  s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
+  s.misc = reinterpret_cast<int*>(s.tslot + 2);
+  s.lutA = reinterpret_cast<uint16_t*>(s.misc + 4);
+  s.lutB = s.lutA + NSL * 128;
+  return s;
+}
 
 struct MxState {           // per-thread copies of the (uniform) pipeline counters
   uint32_t tmem;
@@ -215,35 +254,61 @@ __device__ __forceinline__ void buffer_ready(MxShared& s, MxState& st, int b) {
   }
 }
 
-// row exponents of X (over re and im), column exponents of Y
-__device__ void oz_exponents(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                             MxShared& s) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int r = warp; r < 2 * N; r += nwarp) {
-    int mx = 0;
-    if (r < N) {
-      for (int k = lane; k < N; k += 32) {
-        const double2 v = X[r + (size_t)k * N];
-        mx = max(mx, max(bexp(v.x), bexp(v.y)));
-      }
-    } else {
-      const int j = r - N;
-      for (int k = lane; k < N; k += 32) {
-        const double2 v = Y[k + (size_t)j * N];
-        mx = max(mx, max(bexp(v.x), bexp(v.y)));
-      }
-    }
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    if (lane == 0) {
-      if (r < N) s.expA[r] = mx;
-      else s.expB[r - N] = mx;
-    }
+// fill the digit -> BF16 tables (all threads; a barrier follows before use)
+__device__ __forceinline__ void mx_fill_luts(const MxShared& s) {
+  for (int e = threadIdx.x; e < NSL * 128; e += blockDim.x) {
+    const int p = e >> 7, d = e & 127;
+    s.lutA[e] = (uint16_t)bf16_digit((uint32_t)d, 7 * (3 - (p + 1)), 0u);
+    s.lutB[e] = (uint16_t)bf16_digit((uint32_t)d, 7 * (5 - (p + 1)), 0u);
   }
 }
 
-// digit planes of chunk [k0, k0+16) into buffer b
+// row exponents of X (over re and im), column exponents of Y: biased-exponent
+// maxima by integer max.  Warp w walks columns w, w+8, ... with its lanes on
+// consecutive rows (coalesced); no integer division.
+__device__ void oz_exponents(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
+                             MxShared& s) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int r = threadIdx.x; r < 128; r += blockDim.x) s.expA[r] = 0;
+  __syncthreads();
+  int rmax[4] = {0, 0, 0, 0};
+  for (int k = warp; k < N; k += nwarp) {
+    const double2* xc = X + (size_t)k * N;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = lane + 32 * m;
+      if (i < N) {
+        const double2 v = xc[i];
+        rmax[m] = max(rmax[m], max(bexp(v.x), bexp(v.y)));
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+    if (lane + 32 * m < N) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
+  for (int j = warp; j < N; j += nwarp) {
+    const double2* yc = Y + (size_t)j * N;
+    int cm = 0;
+    for (int k = lane; k < N; k += 32) {
+      const double2 v = yc[k];
+      cm = max(cm, max(bexp(v.x), bexp(v.y)));
+    }
+    cm = __reduce_max_sync(0xffffffffu, cm);
+    if (lane == 0) s.expB[j] = cm;
+  }
+  __syncthreads();
+}
+
+// digit planes of chunk [k0, k0+16) into buffer b: A = all rows of X,
+// B = columns [jb, jb+width) of Y (as rows of the K-major B^T layout)
+__device__ __forceinline__ uint32_t dig2(const uint16_t* lut, unsigned long long f0,
+                                         unsigned long long f1, int sh, uint32_t n0, uint32_t n1) {
+  const uint32_t d0 = (uint32_t)(f0 >> sh) & 127u, d1 = (uint32_t)(f1 >> sh) & 127u;
+  return ((uint32_t)lut[d0] | (n0 << 15)) | (((uint32_t)lut[d1] | (n1 << 15)) << 16);
+}
+
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                            int NP, int k0, const MxShared& s, int b) {
+                            int NP, int k0, int jb, int width, const MxShared& s, int b) {
   unsigned char* A = s.buf[b];
   unsigned char* B = A + 2 * NSL * APLANE;
   const int bplane = NP * KCH * 2;
@@ -257,22 +322,19 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
       if (k0 + kk + 1 < N) x1 = X[i + (size_t)(k0 + kk + 1) * N];
     }
     unsigned n0r, n0i, n1r, n1i;
-    const unsigned long long f0r = fixed42(x0.x, E, n0r), f0i = fixed42(x0.y, E, n0i);
-    const unsigned long long f1r = fixed42(x1.x, E, n1r), f1i = fixed42(x1.y, E, n1i);
+    const unsigned long long f0r = fixed49(x0.x, E, n0r), f0i = fixed49(x0.y, E, n0i);
+    const unsigned long long f1r = fixed49(x1.x, E, n1r), f1i = fixed49(x1.y, E, n1i);
     const int off = (((i >> 3) * 2 + (kk >> 3)) * 64 + (i & 7) * 8 + (kk & 7)) * 2;
 #pragma unroll
     for (int p = 1; p <= NSL; ++p) {
-      const int sh = 7 * (NSL - p), sc = 7 * (3 - p);
-      const uint32_t wr = bf16_digit((uint32_t)(f0r >> sh) & 127u, sc, n0r) |
-                          (bf16_digit((uint32_t)(f1r >> sh) & 127u, sc, n1r) << 16);
-      const uint32_t wi = bf16_digit((uint32_t)(f0i >> sh) & 127u, sc, n0i) |
-                          (bf16_digit((uint32_t)(f1i >> sh) & 127u, sc, n1i) << 16);
-      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1)) * APLANE + off) = wr;
-      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1) + 1) * APLANE + off) = wi;
+      const int sh = 7 * (NSL - p);
+      const uint16_t* lut = s.lutA + (p - 1) * 128;
+      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1)) * APLANE + off) = dig2(lut, f0r, f1r, sh, n0r, n1r);
+      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1) + 1) * APLANE + off) = dig2(lut, f0i, f1i, sh, n0i, n1i);
     }
   }
-  for (int it = threadIdx.x; it < NP * (KCH / 2); it += blockDim.x) {
-    const int kk = 2 * (it & 7), j = it >> 3;
+  for (int it = threadIdx.x; it < width * (KCH / 2); it += blockDim.x) {
+    const int kk = 2 * (it & 7), jl = it >> 3, j = jb + jl;
     double2 y0 = make_double2(0.0, 0.0), y1 = y0;
     int F = 0;
     if (j < N) {
@@ -281,45 +343,50 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
       if (k0 + kk + 1 < N) y1 = Y[(k0 + kk + 1) + (size_t)j * N];
     }
     unsigned n0r, n0i, n1r, n1i;
-    const unsigned long long f0r = fixed42(y0.x, F, n0r), f0i = fixed42(y0.y, F, n0i);
-    const unsigned long long f1r = fixed42(y1.x, F, n1r), f1i = fixed42(y1.y, F, n1i);
-    const int off = (((j >> 3) * 2 + (kk >> 3)) * 64 + (j & 7) * 8 + (kk & 7)) * 2;
+    const unsigned long long f0r = fixed49(y0.x, F, n0r), f0i = fixed49(y0.y, F, n0i);
+    const unsigned long long f1r = fixed49(y1.x, F, n1r), f1i = fixed49(y1.y, F, n1i);
+    const int off = (((jl >> 3) * 2 + (kk >> 3)) * 64 + (jl & 7) * 8 + (kk & 7)) * 2;
 #pragma unroll
     for (int q = 1; q <= NSL; ++q) {
-      const int sh = 7 * (NSL - q), sc = 7 * (4 - q);
-      const uint32_t wr = bf16_digit((uint32_t)(f0r >> sh) & 127u, sc, n0r) |
-                          (bf16_digit((uint32_t)(f1r >> sh) & 127u, sc, n1r) << 16);
-      const uint32_t wi = bf16_digit((uint32_t)(f0i >> sh) & 127u, sc, n0i) |
-                          (bf16_digit((uint32_t)(f1i >> sh) & 127u, sc, n1i) << 16);
-      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1)) * bplane + off) = wr;
-      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1) + 1) * bplane + off) = wi;
+      const int sh = 7 * (NSL - q);
+      const uint16_t* lut = s.lutB + (q - 1) * 128;
+      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1)) * bplane + off) = dig2(lut, f0r, f1r, sh, n0r, n1r);
+      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1) + 1) * bplane + off) = dig2(lut, f0i, f1i, sh, n0i, n1i);
     }
   }
 }
 
-// all slice-pair MMAs of one chunk (thread 0 only)
-__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int pass, bool first) {
+// all slice-pair MMAs of one chunk (thread 0 only).  The descriptors' start
+// address field holds (address >> 4) in its low 14 bits, so a plane offset is
+// added to a base descriptor directly.  Accumulator a = min(t, 6) - 2 sits at
+// tensor-memory column a * width.
+__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int width, int comp,
+                         bool first) {
   const uint32_t A = saddr(s.buf[b]);
   const uint32_t B = A + 2 * NSL * APLANE;
-  const uint32_t bplane = (uint32_t)NP * KCH * 2;
-  bool started[4] = {false, false, false, false};
+  const uint64_t bplane16 = (uint64_t)NP * KCH * 2 >> 4;
+  const uint64_t adesc0 = sdesc(A), bdesc0 = sdesc(B);
+  const uint32_t id_pos = idesc(width, 0), id_neg = idesc(width, 1);
+  unsigned started = 0u;
 #pragma unroll 1
   for (int p = 1; p <= NSL; ++p) {
+    const uint64_t aR = adesc0 + (uint64_t)(2 * (p - 1)) * (APLANE >> 4);
+    const uint64_t aI = aR + (APLANE >> 4);
 #pragma unroll 1
     for (int q = 1; q + p <= NSL + 1; ++q) {
       const int t = p + q;
-      const int a = t <= 4 ? t - 2 : 3;
-      const uint32_t d = tmem + (uint32_t)(a * NP);
-      const uint32_t aR = A + (uint32_t)(2 * (p - 1)) * APLANE, aI = aR + APLANE;
-      const uint32_t bR = B + (uint32_t)(2 * (q - 1)) * bplane, bI = bR + bplane;
-      const uint32_t acc = (first && !started[a]) ? 0u : 1u;
-      started[a] = true;
-      if (pass == 0) {          // Cr = Xr Yr - Xi Yi
-        mma_bf16(d, sdesc(aR), sdesc(bR), idesc(NP, 0), acc);
-        mma_bf16(d, sdesc(aI), sdesc(bI), idesc(NP, 1), 1u);
+      const int a = t <= 5 ? t - 2 : 4;
+      const uint32_t d = tmem + (uint32_t)(a * width);
+      const uint64_t bR = bdesc0 + (uint64_t)(2 * (q - 1)) * bplane16;
+      const uint64_t bI = bR + bplane16;
+      const uint32_t acc = (first && !((started >> a) & 1u)) ? 0u : 1u;
+      started |= 1u << a;
+      if (comp == 0) {          // Cr = Xr Yr - Xi Yi
+        mma_bf16(d, aR, bR, id_pos, acc);
+        mma_bf16(d, aI, bI, id_neg, 1u);
       } else {                  // Ci = Xr Yi + Xi Yr
-        mma_bf16(d, sdesc(aR), sdesc(bI), idesc(NP, 0), acc);
-        mma_bf16(d, sdesc(aI), sdesc(bR), idesc(NP, 0), 1u);
+        mma_bf16(d, aR, bI, id_pos, acc);
+        mma_bf16(d, aI, bR, id_pos, 1u);
       }
     }
   }
@@ -333,21 +400,26 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
                          MxState& st) {
   const int tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
+  const int nsplit = NACC * NP <= 512 ? 1 : 2;
+  const int w0 = nsplit == 1 ? NP : ((NP / 2 + 15) & ~15);
   float nrm = 0.f;
   oz_exponents(X, Y, N, s);
   __syncthreads();
-  for (int pass = 0; pass < 2 && !st.abort; ++pass) {
+  for (int pass = 0; pass < 2 * nsplit && !st.abort; ++pass) {
+    const int comp = pass / nsplit, half = pass % nsplit;
+    const int jb = half == 0 ? 0 : w0;
+    const int width = nsplit == 1 ? NP : (half == 0 ? w0 : NP - w0);
     for (int c = 0; c < nch; ++c) {
       const int b = c & 1;
       buffer_ready(s, st, b);
-      oz_generate(X, Y, N, NP, c * KCH, s, b);
+      oz_generate(X, Y, N, NP, c * KCH, jb, width, s, b);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tc_fence_before();
       st.abort = __syncthreads_or(st.abort);
       tc_fence_after();
       if (st.abort) break;
       if (tid == 0) {
-        oz_issue(s, st.tmem, b, NP, pass, c == 0);
+        oz_issue(s, st.tmem, b, NP, width, comp, c == 0);
         mma_commit(&s.mbar[b]);
       }
       st.ncommit[b] += 1;
@@ -363,50 +435,68 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
     tc_fence_after();
     if (!st.abort) {
       const int warp = tid >> 5, lane = tid & 31;
-      const int quad = warp & 3, half = warp >> 2;
+      const int quad = warp & 3, hw = warp >> 2;
       const int row = quad * 32 + lane;
-      const int cb = half * (NP / 2), ce = cb + NP / 2;
+      const int cb = hw * (width / 2), ce = cb + width / 2;
       const int er = row < N ? s.expA[row] : 0;
       for (int c0 = cb; c0 < ce; c0 += 8) {
-        uint32_t v0[8], v1[8], v2[8], v3[8];
+        uint32_t v[NACC][8];
         const uint32_t ta = st.tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
-        tmem_ld8(ta, v0);
-        tmem_ld8(ta + (uint32_t)NP, v1);
-        tmem_ld8(ta + (uint32_t)(2 * NP), v2);
-        tmem_ld8(ta + (uint32_t)(3 * NP), v3);
+#pragma unroll
+        for (int a = 0; a < NACC; ++a) tmem_ld8(ta + (uint32_t)(a * width), v[a]);
         tmem_wait_ld();
         if (row < N) {
+          double old0[8], old1[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {            // the epilogue's loads first
+            const int j = jb + c0 + jj;
+            const size_t idx = (size_t)row + (size_t)j * N;
+            old0[jj] = 0.0;
+            old1[jj] = 0.0;
+            if (j < N) {
+              if (EPI == OZ_ADD2) {
+                old0[jj] = reinterpret_cast<const double*>(out0 + idx)[comp];
+                old1[jj] = reinterpret_cast<const double*>(out1 + idx)[comp];
+              } else if (EPI == OZ_ADDTO) {
+                old0[jj] = reinterpret_cast<const double*>(src + idx)[comp];
+              } else if ((EPI == OZ_STORE_NORM || EPI == OZ_IMINUS) && comp == 1) {
+                old0[jj] = out0[idx].x;
+              }
+            }
+          }
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
-            const int j = c0 + jj;
-            if (j >= N) break;
-            const long long S = f2ll_int(v0[jj]) + f2ll_int(v1[jj]) + f2ll_int(v2[jj]) +
-                                f2ll_int(v3[jj]);
-            const double val = assemble(S, er + s.expB[j] - 1070);
-            const size_t idx = (size_t)row + (size_t)j * N;
-            double* o0 = reinterpret_cast<double*>(out0 + idx) + pass;
-            if (EPI == OZ_STORE) {
-              *o0 = val;
-            } else if (EPI == OZ_ADD2) {
-              *o0 += val;
-              double* o1 = reinterpret_cast<double*>(out1 + idx) + pass;
-              *o1 += val;
-            } else if (EPI == OZ_STORE_NORM) {
-              *o0 = val;
-              if (pass == 1) {
-                const float re = fabsf(d2f_bits(out0[idx].x)), im = fabsf(d2f_bits(val));
-                const float hi = fmaxf(re, im), lo = fminf(re, im);
-                if (hi > 0.f) {
-                  const float r = lo / hi;
-                  nrm += hi * sqrtf(fmaf(r, r, 1.f));
+            const int j = jb + c0 + jj;
+            if (j < N) {
+              long long S = 0;
+#pragma unroll
+              for (int a = 0; a < NACC; ++a) S += f2ll_int(v[a][jj]);
+              const double val = assemble(S, er + s.expB[j] - 1070);
+              const size_t idx = (size_t)row + (size_t)j * N;
+              double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
+              if (EPI == OZ_STORE) {
+                *o0 = val;
+              } else if (EPI == OZ_ADD2) {
+                *o0 = old0[jj] + val;
+                *(reinterpret_cast<double*>(out1 + idx) + comp) = old1[jj] + val;
+              } else if (EPI == OZ_STORE_NORM) {
+                *o0 = val;
+                if (comp == 1) {
+                  const float re = fabsf(d2f_bits(old0[jj])), im = fabsf(d2f_bits(val));
+                  const float hi = fmaxf(re, im), lo = fminf(re, im);
+                  if (hi > 0.f) {
+                    const float r = lo / hi;
+                    nrm += hi * sqrtf(fmaf(r, r, 1.f));
+                  }
                 }
+              } else if (EPI == OZ_IMINUS) {
+                double w = -val;
+                if (comp == 0 && row == j) w += 1.0;
+                *o0 = w;
+                if (comp == 1) nrm += fabsf(d2f_bits(old0[jj])) + fabsf(d2f_bits(w));
+              } else {   // OZ_ADDTO
+                *o0 = old0[jj] + val;
               }
-            } else if (EPI == OZ_IMINUS) {
-              double v = -val;
-              if (pass == 0 && row == j) v += 1.0;
-              *o0 = v;
-            } else {   // OZ_ADDTO
-              *o0 = reinterpret_cast<const double*>(src + idx)[pass] + val;
             }
           }
         }
@@ -447,12 +537,16 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
   const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
   const int warp = tid >> 5, lane = tid & 31;
   float2* sM = s.gj;
-  for (int e = tid; e < NN; e += T) {
-    const double2 x = X[e];
-    double2 m = make_double2(-x.x, -x.y);
-    if (e % (N + 1) == 0) m = make_double2(w.x - x.x, w.y - x.y);
-    Mi[e] = m;
-    sM[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+  const int nwarp = T >> 5;
+  for (int j = warp; j < N; j += nwarp) {
+    for (int i = lane; i < N; i += 32) {
+      const size_t e = (size_t)i + (size_t)j * N;
+      const double2 x = X[e];
+      double2 m = make_double2(-x.x, -x.y);
+      if (i == j) m = make_double2(w.x - x.x, w.y - x.y);
+      Mi[e] = m;
+      sM[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+    }
   }
   if (tid == 0) s.misc[1] = 0;
   __syncthreads();
@@ -504,17 +598,21 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
       s.rowbuf[j] = nk;
     }
     __syncthreads();
-    for (int e = tid; e < NN; e += T) {
-      const int i = e % N, j = e / N;
-      if (i != k) {
-        float2 v = (j == k) ? make_float2(0.f, 0.f) : sM[e];
-        const float2 f = s.colbuf[i];
-        const float2 rk = s.rowbuf[j];
-        v.x = fmaf(-f.x, rk.x, v.x);
-        v.x = fmaf(f.y, rk.y, v.x);
-        v.y = fmaf(-f.x, rk.y, v.y);
-        v.y = fmaf(-f.y, rk.x, v.y);
-        sM[e] = v;
+    for (int j = warp; j < N; j += nwarp) {
+      const float2 rk = s.rowbuf[j];
+      const bool jk = (j == k);
+      float2* col = sM + j * N;
+#pragma unroll 4
+      for (int i = lane; i < N; i += 32) {
+        if (i != k) {
+          float2 v = jk ? make_float2(0.f, 0.f) : col[i];
+          const float2 f = s.colbuf[i];
+          v.x = fmaf(-f.x, rk.x, v.x);
+          v.x = fmaf(f.y, rk.y, v.x);
+          v.y = fmaf(-f.x, rk.y, v.y);
+          v.y = fmaf(-f.y, rk.x, v.y);
+          col[i] = v;
+        }
       }
     }
     __syncthreads();
@@ -532,30 +630,41 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
     }
   }
   __syncthreads();
-  for (int e = tid; e < NN; e += T) {
-    const int i = e % N, j = e / N;
-    if (singular) {
-      G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
-    } else {
-      const float2 v = sM[i + s.cols[j] * N];
-      G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
+  for (int j = warp; j < N; j += nwarp) {
+    const int cj = s.cols[j];
+    for (int i = lane; i < N; i += 32) {
+      const size_t e = (size_t)i + (size_t)j * N;
+      if (singular) {
+        G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+      } else {
+        const float2 v = sM[i + cj * N];
+        G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
+      }
     }
   }
   __syncthreads();
   return singular;
 }
 
-// (w I - X)^-1 into *Gp: FP32 Gauss-Jordan + ns Newton-Schulz steps on the
-// split tensor-core products.  Uses Mi, R, Gn as work; swaps *Gp and *Gn.
-__device__ int mixed_inverse(const double2* X, double2 w, int N, int NP, int ns, double2** Gp,
+// (w I - X)^-1 into *Gp: FP32 Gauss-Jordan, then Newton-Schulz steps
+// G <- G + G (I - M G) on the split tensor-core products until the residual
+// sum_ij |I - M G|_1 stops shrinking quadratically, or is at most 1e-7 N
+// before an update (after which the residual is ~(1e-7)^2, below the products'
+// own rounding); at most ns_max steps.  Uses Mi, R, Gn as work; swaps *Gp and *Gn.
+__device__ int mixed_inverse(const double2* X, double2 w, int N, int NP, int ns_max, double2** Gp,
                              double2** Gnp, double2* Mi, double2* R, MxShared& s, MxState& st) {
   const int sing = gj32_start(X, w, N, Mi, *Gp, s);
-  for (int t = 0; t < ns && !st.abort; ++t) {
-    oz_gemm<OZ_IMINUS>(Mi, *Gp, N, NP, R, nullptr, nullptr, s, st);      // R = I - M G
-    oz_gemm<OZ_ADDTO>(*Gp, R, N, NP, *Gnp, nullptr, *Gp, s, st);         // Gn = G + G R
+  float prev = 3.0e38f;
+  for (int t = 0; t < ns_max && !st.abort; ++t) {
+    const float part = oz_gemm<OZ_IMINUS>(Mi, *Gp, N, NP, R, nullptr, nullptr, s, st);  // R = I - M G
+    const float res = block_sum_f(part, s);
+    if (!(res < 0.25f * prev)) break;                 // no longer converging (or NaN)
+    oz_gemm<OZ_ADDTO>(*Gp, R, N, NP, *Gnp, nullptr, *Gp, s, st);                         // Gn = G + G R
     double2* tmp = *Gp;
     *Gp = *Gnp;
     *Gnp = tmp;
+    if (res <= 1e-7f * (float)N) break;               // G + G R is then at the products' accuracy
+    prev = res;
   }
   return sing;
 }
@@ -565,23 +674,8 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
   const int NP = (N + 15) & ~15;
-  const int bufbytes = 2 * NSL * APLANE + 2 * NSL * NP * KCH * 2;
-  MxShared s;
-  s.buf[0] = smraw;
-  s.buf[1] = smraw + bufbytes;
-  s.gj = reinterpret_cast<float2*>(smraw);
-  unsigned char* tail = smraw + 2 * bufbytes;
-  s.colbuf = reinterpret_cast<float2*>(tail);
-  s.rowbuf = s.colbuf + 128;
-  s.recip = s.rowbuf + 128;
-  s.perm = reinterpret_cast<int*>(s.recip + 2);
-  s.cols = s.perm + 128;
-  s.expA = s.cols + 128;
-  s.expB = s.expA + 128;
-  s.red = reinterpret_cast<float*>(s.expB + 128);
-  s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
-  s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
-  s.misc = reinterpret_cast<int*>(s.tslot + 2);
+  MxShared s = mx_layout(smraw, NP);
+  mx_fill_luts(s);
 
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
@@ -666,22 +760,35 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
     if (mixed_inverse(ES, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
     if (a.gll)
       for (int e = tid; e < NN; e += T) a.gll[(size_t)inst * NN + e] = G[e];
-    if (tid == 0)
+    double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (tid == 0) {
       for (int q = 0; q < a.ntop; ++q) {
         const int io = a.top[q] - 1;
         const double v = G[io + (size_t)io * N].y;
         dl = a.divide_by_pi ? dl - v / PI_REF : dl - v;
       }
+      if (a.spin[0])
+        spin_sums([&](int i, int j) { return G[i + (size_t)j * N]; }, a.nw, a.ntop, a.top, 0,
+                  a.divide_by_pi, spin[0], spin[1], spin[2]);
+    }
     __syncthreads();
     if (mixed_inverse(ET, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
     if (a.grr)
       for (int e = tid; e < NN; e += T) a.grr[(size_t)inst * NN + e] = G[e];
-    if (tid == 0)
+    if (tid == 0) {
       for (int q = 0; q < a.nbot; ++q) {
         const int io = N - a.nw + a.bot[q] - 1;
         const double v = G[io + (size_t)io * N].y;
         dr = a.divide_by_pi ? dr - v / PI_REF : dr - v;
       }
+      if (a.spin[0]) {
+        auto gr = [&](int i, int j) { return G[i + (size_t)j * N]; };
+        if (a.spin_right_bottom)
+          spin_sums(gr, a.nw, a.nbot, a.bot, N - a.nw, a.divide_by_pi, spin[3], spin[4], spin[5]);
+        else
+          spin_sums(gr, a.nw, a.ntop, a.top, 0, a.divide_by_pi, spin[3], spin[4], spin[5]);
+      }
+    }
     __syncthreads();
     if (mixed_inverse(E, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
     if (a.gb)
@@ -696,6 +803,8 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
       a.dos_l[oidx] = dl;
       a.dos_r[oidx] = dr;
       a.dos_bulk[oidx] = db;
+      if (a.spin[0])
+        for (int c = 0; c < 6; ++c) a.spin[c][oidx] = spin[c];
       if (a.iters) a.iters[oidx] = it;
       if (a.status) a.status[oidx] = (uint8_t)stat;
     }
@@ -718,23 +827,8 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int NP = (N + 15) & ~15;
   const int NN = N * N;
-  const int bufbytes = 2 * NSL * APLANE + 2 * NSL * NP * KCH * 2;
-  MxShared s;
-  s.buf[0] = smraw;
-  s.buf[1] = smraw + bufbytes;
-  s.gj = reinterpret_cast<float2*>(smraw);
-  unsigned char* tail = smraw + 2 * bufbytes;
-  s.colbuf = reinterpret_cast<float2*>(tail);
-  s.rowbuf = s.colbuf + 128;
-  s.recip = s.rowbuf + 128;
-  s.perm = reinterpret_cast<int*>(s.recip + 2);
-  s.cols = s.perm + 128;
-  s.expA = s.cols + 128;
-  s.expB = s.expA + 128;
-  s.red = reinterpret_cast<float*>(s.expB + 128);
-  s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
-  s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
-  s.misc = reinterpret_cast<int*>(s.tslot + 2);
+  MxShared s = mx_layout(smraw, NP);
+  mx_fill_luts(s);
   const int tid = threadIdx.x;
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
@@ -782,15 +876,14 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
 size_t mixed_smem(int N) {
   const int NP = (N + 15) & ~15;
   const size_t bufbytes = 2 * NSL * APLANE + 2 * NSL * (size_t)NP * KCH * 2;
-  size_t planes = 2 * bufbytes;
-  const size_t gj = (size_t)N * N * sizeof(float2);
-  if (gj > planes) planes = gj;
-  return planes + 128 * 8 * 2 + 16 + 128 * 4 * 4 + 32 * 4 + 16 + 8 + 16;
+  // the FP32 Gauss-Jordan matrix (N*N float2) aliases the buffers
+  const size_t planes = 2 * bufbytes > (size_t)N * N * 8 ? 2 * bufbytes : (size_t)N * N * 8;
+  return planes + 128 * 8 * 2 + 16 + 128 * 4 * 4 + 32 * 4 + 16 + 8 + 16 + 2 * NSL * 128 * 2;
 }
 
 }  // namespace
 
-int decim_mixed_max_n() { return 128; }
+int decim_mixed_max_n() { return 112; }     // double-buffered 7-digit planes fill shared memory
 
 size_t decim_mixed_ws_matrices() { return 11; }
 
@@ -812,7 +905,7 @@ cudaError_t decim_mixed_config(int N, DecimConfig* cfg) {
 
 cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                   cudaStream_t s) {
-  k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 2, 3);
+  k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 6, 8);
   return cudaGetLastError();
 }
 
