@@ -124,3 +124,41 @@ def test_spin_mixed(built_lib):
     scale = np.abs(ref["dos_l"]).max()
     for name in ("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r"):
         assert np.max(np.abs(got[name] - ref[name])) <= 1e-6 * scale, name
+
+
+def _oracle_point(args):
+    from oracle import wt_oracle as Ow
+    from wannier_tools_gb300 import synthetic as S
+    nw, np_, seed, k, om, eta = args
+    m = S.make_model(nw, np_, seed=seed)
+    top = list(range(1, nw + 1))
+    r = Ow.surface_spectrum(m.hmnr, m.irvec, m.ndegen, nw, np_, k, om, eta, top, top,
+                            scale=1.0 / Ow.PI_REF)
+    return {n: r[n] for n in ("dos_l", "dos_r", "dos_bulk", "iters")}
+
+
+def test_spectrum_mixed_arc_plane_dense(built_lib):
+    """192 points spread over the 201 x 201 Fermi-arc plane of the Ndim = 112
+    model (eta = 1e-3 eV, every orbital in both lists): every point within
+    1e-5 of the FP64 oracle.  Points near poles need more than one in-loop
+    refinement step; a fixed single step leaves errors near 3e-4 here."""
+    import multiprocessing as mp
+    import os
+    nw, np_, seed, eta = 56, 2, 2024, 1e-3 * EV
+    _, _, kall = api.kplane_slab(201, 201, (-0.5, -0.5), (1.0, 0.0), (0.0, 1.0))
+    idx = np.arange(192) * (len(kall) // 192)
+    kp = kall[idx]
+    om = np.array([0.0])
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        parts = pool.map(_oracle_point, [(nw, np_, seed, kp[[i]], om, eta) for i in range(len(kp))])
+    ref = {n: np.concatenate([p[n] for p in parts]) for n in ("dos_l", "dos_r", "dos_bulk", "iters")}
+    m = synthetic.make_model(nw, np_, seed=seed)
+    top = list(range(1, nw + 1))
+    with api.Model.from_surface_model(m) as g:
+        got = g.surface_spectrum(kp, om, eta, top, top, divide_by_pi=True, precision=PREC_MIXED)
+    for name in ("dos_l", "dos_r", "dos_bulk"):
+        e = _rel(got[name].ravel(), ref[name].ravel())
+        print("dense arc plane", name, e)
+        assert e <= 1e-5, (name, e)
+    assert (got["status"] == 0).all()

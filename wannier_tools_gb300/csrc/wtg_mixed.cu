@@ -309,15 +309,25 @@ __device__ __forceinline__ uint32_t dig2(const uint16_t* lut, unsigned long long
 
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
                             int NP, int k0, int jb, int width, const MxShared& s, int b) {
-  unsigned char* A = s.buf[b];
-  unsigned char* B = A + 2 * NSL * APLANE;
+  unsigned char* __restrict__ A = s.buf[b];
+  unsigned char* __restrict__ B = A + 2 * NSL * APLANE;
+  const int* __restrict__ expA = s.expA;
+  const int* __restrict__ expB = s.expB;
+  const uint16_t* __restrict__ lutA = s.lutA;
+  const uint16_t* __restrict__ lutB = s.lutB;
   const int bplane = NP * KCH * 2;
   for (int it = threadIdx.x; it < 128 * (KCH / 2); it += blockDim.x) {
     const int i = it & 127, kk = 2 * (it >> 7);
+    if (i >= N) {                                  // padding rows of the M = 128 tile
+      const int off = (((i >> 3) * 2 + (kk >> 3)) * 64 + (i & 7) * 8 + (kk & 7)) * 2;
+#pragma unroll
+      for (int pl = 0; pl < 2 * NSL; ++pl) *reinterpret_cast<uint32_t*>(A + pl * APLANE + off) = 0u;
+      continue;
+    }
     double2 x0 = make_double2(0.0, 0.0), x1 = x0;
     int E = 0;
     if (i < N) {
-      E = s.expA[i];
+      E = expA[i];
       if (k0 + kk < N) x0 = X[i + (size_t)(k0 + kk) * N];
       if (k0 + kk + 1 < N) x1 = X[i + (size_t)(k0 + kk + 1) * N];
     }
@@ -328,17 +338,23 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 #pragma unroll
     for (int p = 1; p <= NSL; ++p) {
       const int sh = 7 * (NSL - p);
-      const uint16_t* lut = s.lutA + (p - 1) * 128;
+      const uint16_t* lut = lutA + (p - 1) * 128;
       *reinterpret_cast<uint32_t*>(A + (2 * (p - 1)) * APLANE + off) = dig2(lut, f0r, f1r, sh, n0r, n1r);
       *reinterpret_cast<uint32_t*>(A + (2 * (p - 1) + 1) * APLANE + off) = dig2(lut, f0i, f1i, sh, n0i, n1i);
     }
   }
   for (int it = threadIdx.x; it < width * (KCH / 2); it += blockDim.x) {
     const int kk = 2 * (it & 7), jl = it >> 3, j = jb + jl;
+    if (j >= N) {                                  // padding columns
+      const int off = (((jl >> 3) * 2 + (kk >> 3)) * 64 + (jl & 7) * 8 + (kk & 7)) * 2;
+#pragma unroll
+      for (int pl = 0; pl < 2 * NSL; ++pl) *reinterpret_cast<uint32_t*>(B + pl * bplane + off) = 0u;
+      continue;
+    }
     double2 y0 = make_double2(0.0, 0.0), y1 = y0;
     int F = 0;
     if (j < N) {
-      F = s.expB[j];
+      F = expB[j];
       if (k0 + kk < N) y0 = Y[(k0 + kk) + (size_t)j * N];
       if (k0 + kk + 1 < N) y1 = Y[(k0 + kk + 1) + (size_t)j * N];
     }
@@ -349,7 +365,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 #pragma unroll
     for (int q = 1; q <= NSL; ++q) {
       const int sh = 7 * (NSL - q);
-      const uint16_t* lut = s.lutB + (q - 1) * 128;
+      const uint16_t* lut = lutB + (q - 1) * 128;
       *reinterpret_cast<uint32_t*>(B + (2 * (q - 1)) * bplane + off) = dig2(lut, f0r, f1r, sh, n0r, n1r);
       *reinterpret_cast<uint32_t*>(B + (2 * (q - 1) + 1) * bplane + off) = dig2(lut, f0i, f1i, sh, n0i, n1i);
     }
@@ -361,7 +377,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 // added to a base descriptor directly.  Accumulator a = min(t, 6) - 2 sits at
 // tensor-memory column a * width.
 __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int width, int comp,
-                         bool first) {
+                         bool first, uint32_t bank) {
   const uint32_t A = saddr(s.buf[b]);
   const uint32_t B = A + 2 * NSL * APLANE;
   const uint64_t bplane16 = (uint64_t)NP * KCH * 2 >> 4;
@@ -376,7 +392,7 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int wi
     for (int q = 1; q + p <= NSL + 1; ++q) {
       const int t = p + q;
       const int a = t <= 5 ? t - 2 : 4;
-      const uint32_t d = tmem + (uint32_t)(a * width);
+      const uint32_t d = tmem + bank + (uint32_t)(a * width);
       const uint64_t bR = bdesc0 + (uint64_t)(2 * (q - 1)) * bplane16;
       const uint64_t bI = bR + bplane16;
       const uint32_t acc = (first && !((started >> a) & 1u)) ? 0u : 1u;
@@ -400,13 +416,18 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
                          MxState& st) {
   const int tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
+  // both components in one pass when their accumulators fit tensor memory
+  // (Ndim <= 48), else one component per pass over one or two column halves
+  const bool both = 2 * NACC * NP <= 512;
   const int nsplit = NACC * NP <= 512 ? 1 : 2;
   const int w0 = nsplit == 1 ? NP : ((NP / 2 + 15) & ~15);
+  const int npass = both ? 1 : 2 * nsplit;
   float nrm = 0.f;
   oz_exponents(X, Y, N, s);
   __syncthreads();
-  for (int pass = 0; pass < 2 * nsplit && !st.abort; ++pass) {
-    const int comp = pass / nsplit, half = pass % nsplit;
+  for (int pass = 0; pass < npass && !st.abort; ++pass) {
+    const int comp0 = both ? 0 : pass / nsplit, comp1 = both ? 1 : comp0;
+    const int half = both ? 0 : pass % nsplit;
     const int jb = half == 0 ? 0 : w0;
     const int width = nsplit == 1 ? NP : (half == 0 ? w0 : NP - w0);
     for (int c = 0; c < nch; ++c) {
@@ -419,7 +440,9 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
       tc_fence_after();
       if (st.abort) break;
       if (tid == 0) {
-        oz_issue(s, st.tmem, b, NP, width, comp, c == 0);
+        for (int comp = comp0; comp <= comp1; ++comp)
+          oz_issue(s, st.tmem, b, NP, width, comp, c == 0,
+                   (uint32_t)((comp - comp0) * NACC * width));
         mma_commit(&s.mbar[b]);
       }
       st.ncommit[b] += 1;
@@ -433,15 +456,17 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
     }
     st.abort = __syncthreads_or(st.abort);
     tc_fence_after();
-    if (!st.abort) {
+    const int* __restrict__ expB = s.expB;
+    for (int comp = comp0; comp <= comp1 && !st.abort; ++comp) {
       const int warp = tid >> 5, lane = tid & 31;
       const int quad = warp & 3, hw = warp >> 2;
       const int row = quad * 32 + lane;
       const int cb = hw * (width / 2), ce = cb + width / 2;
       const int er = row < N ? s.expA[row] : 0;
+      const uint32_t bank = (uint32_t)((comp - comp0) * NACC * width);
       for (int c0 = cb; c0 < ce; c0 += 8) {
         uint32_t v[NACC][8];
-        const uint32_t ta = st.tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
+        const uint32_t ta = st.tmem + bank + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
 #pragma unroll
         for (int a = 0; a < NACC; ++a) tmem_ld8(ta + (uint32_t)(a * width), v[a]);
         tmem_wait_ld();
@@ -471,7 +496,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
               long long S = 0;
 #pragma unroll
               for (int a = 0; a < NACC; ++a) S += f2ll_int(v[a][jj]);
-              const double val = assemble(S, er + s.expB[j] - 1070);
+              const double val = assemble(S, er + expB[j] - 1070);
               const size_t idx = (size_t)row + (size_t)j * N;
               double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
               if (EPI == OZ_STORE) {
@@ -533,11 +558,18 @@ __device__ __forceinline__ long long cabs1_key_f(float2 v) {
 // M = w I - X (FP64, kept in Mi for the refinement), then FP32 Gauss-Jordan
 // into G (FP64).  Returns 1 on an exact zero pivot (G = identity then).
 __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, double2* Mi,
-                          double2* G, MxShared& s) {
-  const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
-  const int warp = tid >> 5, lane = tid & 31;
-  float2* sM = s.gj;
-  const int nwarp = T >> 5;
+                          double2* G, MxShared& s_) {
+  const int T = blockDim.x, tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
+  // local copies of the shared-memory pointers (kept in registers)
+  float2* __restrict__ sM = s_.gj;
+  float2* __restrict__ colbuf = s_.colbuf;
+  float2* __restrict__ rowbuf = s_.rowbuf;
+  float2* __restrict__ recip = s_.recip;
+  int* __restrict__ perm = s_.perm;
+  int* __restrict__ cols = s_.cols;
+  int* __restrict__ misc = s_.misc;
+  const int LD = N + 1;                 // odd leading dimension: row walks hit distinct banks
   for (int j = warp; j < N; j += nwarp) {
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
@@ -545,17 +577,17 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
       double2 m = make_double2(-x.x, -x.y);
       if (i == j) m = make_double2(w.x - x.x, w.y - x.y);
       Mi[e] = m;
-      sM[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+      sM[i + j * LD] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
     }
   }
-  if (tid == 0) s.misc[1] = 0;
+  if (tid == 0) misc[1] = 0;
   __syncthreads();
   for (int k = 0; k < N; ++k) {
     if (warp == 0) {
       long long best = -1;
       int bi = N;
       for (int i = k + lane; i < N; i += 32) {
-        const long long v = cabs1_key_f(sM[i + k * N]);
+        const long long v = cabs1_key_f(sM[i + k * LD]);
         if (v > best) {
           best = v;
           bi = i;
@@ -571,73 +603,79 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
         }
       }
       const int p = bi;
-      for (int i = lane; i < N; i += 32) s.colbuf[i] = sM[(i == p ? k : i) + k * N];
+      for (int i = lane; i < N; i += 32) colbuf[i] = sM[(i == p ? k : i) + k * LD];
       if (lane == 0) {
-        s.perm[k] = p;
+        perm[k] = p;
         if (best == 0) {
-          s.misc[1] = 1;
+          misc[1] = 1;
         } else {
-          const float2 pv = sM[p + k * N];
+          const float2 pv = sM[p + k * LD];
           const float inv_d = 1.0f / (pv.x * pv.x + pv.y * pv.y);
-          s.recip[0] = make_float2(pv.x * inv_d, -pv.y * inv_d);
+          recip[0] = make_float2(pv.x * inv_d, -pv.y * inv_d);
         }
       }
     }
     __syncthreads();
-    if (s.misc[1]) break;
-    const int p = s.perm[k];
-    const float2 r = s.recip[0];
+    if (misc[1]) break;
+    const int p = perm[k];
+    const float2 r = recip[0];
     for (int j = tid; j < N; j += T) {
-      const float2 akj = sM[k + j * N];
-      const float2 apj = sM[p + j * N];
-      if (p != k) sM[p + j * N] = akj;
+      const float2 akj = sM[k + j * LD];
+      const float2 apj = sM[p + j * LD];
+      if (p != k) sM[p + j * LD] = akj;
       const float2 nk = (j == k) ? r
                                  : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
                                                fmaf(apj.x, r.y, apj.y * r.x));
-      sM[k + j * N] = nk;
-      s.rowbuf[j] = nk;
+      sM[k + j * LD] = nk;
+      rowbuf[j] = nk;
     }
     __syncthreads();
+    float2 f[4];                          // this lane's multipliers, rows lane + 32 m
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = lane + 32 * m;
+      f[m] = (i < N && i != k) ? colbuf[i] : make_float2(0.f, 0.f);
+    }
     for (int j = warp; j < N; j += nwarp) {
-      const float2 rk = s.rowbuf[j];
+      const float2 rk = rowbuf[j];
       const bool jk = (j == k);
-      float2* col = sM + j * N;
-#pragma unroll 4
-      for (int i = lane; i < N; i += 32) {
-        if (i != k) {
+      float2* col = sM + j * LD;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int i = lane + 32 * m;
+        if (i < N && i != k) {
           float2 v = jk ? make_float2(0.f, 0.f) : col[i];
-          const float2 f = s.colbuf[i];
-          v.x = fmaf(-f.x, rk.x, v.x);
-          v.x = fmaf(f.y, rk.y, v.x);
-          v.y = fmaf(-f.x, rk.y, v.y);
-          v.y = fmaf(-f.y, rk.x, v.y);
+          v.x = fmaf(-f[m].x, rk.x, v.x);
+          v.x = fmaf(f[m].y, rk.y, v.x);
+          v.y = fmaf(-f[m].x, rk.y, v.y);
+          v.y = fmaf(-f[m].y, rk.x, v.y);
           col[i] = v;
         }
       }
     }
     __syncthreads();
   }
-  const int singular = s.misc[1];
+  const int singular = misc[1];
   if (tid == 0) {
-    for (int j = 0; j < N; ++j) s.cols[j] = j;
+    for (int j = 0; j < N; ++j) cols[j] = j;
     if (!singular) {
       for (int k = N - 1; k >= 0; --k) {
-        const int p = s.perm[k];
-        const int t = s.cols[k];
-        s.cols[k] = s.cols[p];
-        s.cols[p] = t;
+        const int p = perm[k];
+        const int t = cols[k];
+        cols[k] = cols[p];
+        cols[p] = t;
       }
     }
   }
   __syncthreads();
   for (int j = warp; j < N; j += nwarp) {
-    const int cj = s.cols[j];
+    const int cj = cols[j];
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
       if (singular) {
         G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
       } else {
-        const float2 v = sM[i + cj * N];
+        const float2 v = sM[i + cj * LD];
         G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
       }
     }
@@ -645,6 +683,7 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
   __syncthreads();
   return singular;
 }
+
 
 // (w I - X)^-1 into *Gp: FP32 Gauss-Jordan, then Newton-Schulz steps
 // G <- G + G (I - M G) on the split tensor-core products until the residual
@@ -877,7 +916,7 @@ size_t mixed_smem(int N) {
   const int NP = (N + 15) & ~15;
   const size_t bufbytes = 2 * NSL * APLANE + 2 * NSL * (size_t)NP * KCH * 2;
   // the FP32 Gauss-Jordan matrix (N*N float2) aliases the buffers
-  const size_t planes = 2 * bufbytes > (size_t)N * N * 8 ? 2 * bufbytes : (size_t)N * N * 8;
+  const size_t planes = 2 * bufbytes > (size_t)(N + 1) * N * 8 ? 2 * bufbytes : (size_t)(N + 1) * N * 8;
   return planes + 128 * 8 * 2 + 16 + 128 * 4 * 4 + 32 * 4 + 16 + 8 + 16 + 2 * NSL * 128 * 2;
 }
 
