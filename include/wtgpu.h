@@ -57,11 +57,12 @@ extern "C" {
                                    the point's outputs are not valid */
 
 /* precision modes */
-#define WTG_PREC_FP64  0        /* all-FP64 decimation (FP64 DFMA pipe) */
+#define WTG_PREC_FP64  0        /* all-FP64 decimation (FP64 DFMA pipe); Ndim <= 320 (above
+                                   119 the inverse runs in global memory) */
 #define WTG_PREC_MIXED 1        /* products as exact BF16 digit splits on the tcgen05 tensor
-                                   cores (42-bit operands, FP32 accumulation exact per slice
+                                   cores (49-bit operands, FP32 accumulation exact per slice
                                    order, int64 recombination), inverses FP32 Gauss-Jordan +
-                                   Newton-Schulz refinement on those products; Ndim <= 128 */
+                                   Newton-Schulz refinement on those products; Ndim <= 112 */
 
 typedef struct wtg_model* wtg_model_t;
 

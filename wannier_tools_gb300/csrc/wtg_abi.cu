@@ -103,7 +103,7 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
                  double* const* d_spin = nullptr, int spin_right_bottom = 0) {
   const int N = m->N;
   const bool mixed = precision == WTG_PREC_MIXED;
-  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_max_n();
+  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_large_max_n();
   if (N > nmax)
     return fail(WTG_EUNSUPPORTED, "Ndim " + std::to_string(N) + " exceeds the " +
                                       (mixed ? "mixed" : "FP64") + " kernel limit " +
@@ -114,9 +114,10 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
   if (mixed) {
     WTG_CK(wtg::decim_mixed_config(N, &cfg));
   } else {
-    WTG_CK(wtg::decim_fp64_config(N, thr, &cfg));
+    const char* gi = getenv("WTG_FP64_GLOBAL_INVERSE");   // testing: force the large-Ndim variant
+    WTG_CK(wtg::decim_fp64_config(N, thr, &cfg, gi && atoi(gi) != 0));
   }
-  const size_t ws_mats = mixed ? wtg::decim_mixed_ws_matrices() : 8;
+  const size_t ws_mats = mixed ? wtg::decim_mixed_ws_matrices() : wtg::decim_fp64_ws_matrices(cfg);
   if (cfg.ctas_per_sm < 1) return fail(WTG_EUNSUPPORTED, "decimation kernel does not fit an SM");
   int nsm = 0;
   WTG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, m->device));
@@ -372,7 +373,7 @@ int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00, co
                        int* status) {
   if (ndim < 1 || !h00 || !h01 || !gll || !grr || !gb) return fail(WTG_EINVAL, "bad argument");
   if (itermax < 0) return fail(WTG_EINVAL, "itermax < 0");
-  if (ndim > wtg::decim_fp64_max_n())
+  if (ndim > wtg::decim_fp64_large_max_n())
     return fail(WTG_EUNSUPPORTED, "Ndim exceeds the FP64 kernel limit");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
@@ -380,8 +381,9 @@ int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00, co
   const size_t nn = (size_t)ndim * ndim;
   wtg::DecimConfig cfg;
   WTG_CK(wtg::decim_fp64_config(ndim, 0, &cfg));
-  // one allocation: h[2nn] | gll gll grr gb [3nn] | ws [8nn] | omega | outputs
-  const size_t bytes = sizeof(double2) * (13 * nn) + 64 + 64;
+  // one allocation: h[2nn] | gll grr gb [3nn] | ws [8 or 9 nn] | omega | outputs
+  const size_t wsm = wtg::decim_fp64_ws_matrices(cfg);
+  const size_t bytes = sizeof(double2) * ((5 + wsm) * nn) + 64 + 64;
   char* base = nullptr;
   WTG_CK(cudaMalloc(&base, bytes));
   double2* dh = (double2*)base;
@@ -389,7 +391,7 @@ int wtg_surfgreen_1985(int ndim, double omega, double eta, const double* h00, co
   double2* dgrr = dgll + nn;
   double2* dgb = dgrr + nn;
   double2* dws = dgb + nn;
-  char* tail = (char*)(dws + 8 * nn);
+  char* tail = (char*)(dws + wsm * nn);
   double* dw = (double*)tail;          // omega
   double* ddos = dw + 1;               // 3 doubles
   int* dctr = (int*)(ddos + 3);
@@ -514,7 +516,7 @@ static int unit_op(int op, int n, const double* a, const double* b, double* c, i
   if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
     return fail(WTG_EINVAL, "unknown precision mode");
   const bool mixed = precision == WTG_PREC_MIXED;
-  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_max_n();
+  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_large_max_n();
   if (n > nmax) return fail(WTG_EUNSUPPORTED, "n exceeds the kernel limit " + std::to_string(nmax));
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)

@@ -110,7 +110,7 @@ struct DecimArgs {
   double2* gll;               // optional full outputs [n_inst][N*N] (null = skip)
   double2* grr;
   double2* gb;
-  double2* ws;                // [grid][8][N*N] workspace
+  double2* ws;                // [grid][8 or 9][N*N] workspace (decim_fp64_ws_matrices)
   int* counter;               // work counter, zero at launch
   int KC;                     // GEMM k-chunk staged in shared memory
   int ntop, nbot;
@@ -124,12 +124,21 @@ struct DecimConfig {
   int RP;                     // register rows per pass in the GEMM (template)
   size_t smem;                // dynamic shared memory per CTA
   int ctas_per_sm;
+  int inv_global = 0;         // FP64: 1 = the inverse runs in global memory (large Ndim)
 };
 
 // Largest Ndim the shared-memory Gauss-Jordan kernel takes.
 int decim_fp64_max_n();
-// Launch shape for a given N on the current device (threads override: 0 = auto).
-cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg);
+// Largest Ndim of the FP64 kernel whose inverse runs in global memory (above decim_fp64_max_n).
+int decim_fp64_large_max_n();
+// N x N complex workspace matrices per CTA of the FP64 kernel in this configuration (8, or 9
+// when the inverse runs in global memory).
+size_t decim_fp64_ws_matrices(const DecimConfig& cfg);
+// Launch shape for a given N on the current device (threads override: 0 = auto).  The inverse
+// runs in global memory above decim_fp64_max_n(), or at any N with force_global (the two
+// variants agree bit for bit).
+cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg,
+                              bool force_global = false);
 cudaError_t launch_decimate_fp64(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                  cudaStream_t s);
 
@@ -142,11 +151,11 @@ cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, in
                                   cudaStream_t s);
 
 // One product (op 0: C = X*Y) or inverse (op 1: C = X^-1) by a single CTA.
-// Mixed: ws holds 5 N x N complex matrices; FP64: negX holds one.
+// Mixed: ws holds 5 N x N complex matrices; FP64: work holds two.
 cudaError_t launch_mixed_unit(int op, int N, const double2* X, const double2* Y, double2* C,
                               double2* ws, int ns, int* status, cudaStream_t s);
 cudaError_t launch_fp64_unit(int op, int N, const double2* X, const double2* Y, double2* C,
-                             double2* negX, int* status, cudaStream_t s);
+                             double2* work, int* status, cudaStream_t s);
 
 // Sets the calling thread's message returned by wtg_last_error.
 void set_last_error(const char* msg);

@@ -29,24 +29,16 @@ namespace {
 
 #include "wtg_fp64_dev.cuh"
 
-template <int RP>
-__global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
+// GI = false: the inverse runs in shared memory (Ndim <= decim_fp64_max_n());
+// GI = true: it runs in a ninth workspace matrix in global memory, in panels
+// (gj_invert_global; Ndim <= 320).
+template <int RP, bool GI>
+__global__ void __launch_bounds__(GI ? 256 : 512, 1) k_decimate_fp64(const DecimArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
-  const size_t big = (size_t)max(NN, 2 * N * a.KC);
-  Shared s;
-  s.big = reinterpret_cast<double2*>(smraw);
-  s.sX = s.big;
-  s.sY = s.big + (size_t)N * a.KC;
-  s.colbuf = s.big + big;
-  s.rowbuf = s.colbuf + N;
-  s.recip = s.rowbuf + N;
-  s.red = reinterpret_cast<double*>(s.recip + 2);
-  s.perm = reinterpret_cast<int*>(s.red + 32);
-  s.cols = s.perm + N;
-  s.misc = s.cols + N;
-
-  double2* W = a.ws + (size_t)blockIdx.x * 8 * NN;
+  const Shared s = fp64_layout(smraw, N, a.KC, !GI);
+  double2* W = a.ws + (size_t)blockIdx.x * (GI ? 9 : 8) * NN;
+  double2* Mg = GI ? W + (size_t)8 * NN : nullptr;   // global-memory inverse work
   double2* E = W;
   double2* ES = W + (size_t)NN;
   double2* ET = W + (size_t)2 * NN;
@@ -63,6 +55,21 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
     const double2* H00 = a.h + (size_t)ik * 2 * NN;
     const double2* H01 = H00 + NN;
     const double2 w = make_double2(a.omega[iw], a.eta);     // src/surfgreen.f90:82
+    // (w - X)^-1, optionally stored un-permuted to out; ginv reads the result
+    auto invert = [&](const double2* X, double2* out) -> int {
+      int sing;
+      if (GI) {
+        sing = gj_invert_global(X, w, N, Mg, s);
+        if (out) gj_store_global(N, Mg, s, out);
+      } else {
+        sing = gj_invert(X, w, N, s);
+        if (out) gj_store(N, s, out);
+      }
+      return sing;
+    };
+    auto ginv = [&](int i, int j) {
+      return GI ? Mg[i + (size_t)s.cols[j] * N] : s.big[i + s.cols[j] * N];
+    };
 
     double2* Al = bufs[0];
     double2* Be = bufs[1];
@@ -85,8 +92,7 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
     bool conv = false;
     for (int itc = 1; itc <= a.itermax; ++itc) {              // src/surfgreen.f90:86
       it = itc;
-      if (gj_invert(E, w, N, s)) st |= PT_SINGULAR;           // :88-89
-      gj_store(N, s, G);
+      if (invert(E, G)) st |= PT_SINGULAR;                    // :88-89
       __syncthreads();
       cta_gemm<RP, EPI_STORE>(Al, G, N, a.KC, s.sX, s.sY, M1, nullptr);    // :92
       cta_gemm<RP, EPI_STORE>(Be, G, N, a.KC, s.sX, s.sY, M2, nullptr);    // :95
@@ -112,44 +118,40 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
     const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
     double dl = 0.0, dr = 0.0, db = 0.0;
     // GLL = (w - eps_s)^-1                                   // :127-128
-    if (gj_invert(ES, w, N, s)) st |= PT_SINGULAR;
-    if (a.gll) gj_store(N, s, a.gll + (size_t)inst * NN);
+    if (invert(ES, a.gll ? a.gll + (size_t)inst * NN : nullptr)) st |= PT_SINGULAR;
     double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (tid == 0) {
       for (int q = 0; q < a.ntop; ++q) {
         const int io = a.top[q] - 1;
-        const double v = gj_diag(N, s, io).y;
+        const double v = ginv(io, io).y;
         dl = a.divide_by_pi ? dl - v / PI_REF : dl - v;
       }
       if (a.spin[0])                                          // src/surfstat.f90:162-177
-        spin_sums([&](int i, int j) { return s.big[i + s.cols[j] * N]; }, a.nw, a.ntop, a.top, 0,
+        spin_sums(ginv, a.nw, a.ntop, a.top, 0,
                   a.divide_by_pi, spin[0], spin[1], spin[2]);
     }
     __syncthreads();
     // GRR = (w - eps_t)^-1                                   // :130-131
-    if (gj_invert(ET, w, N, s)) st |= PT_SINGULAR;
-    if (a.grr) gj_store(N, s, a.grr + (size_t)inst * NN);
+    if (invert(ET, a.grr ? a.grr + (size_t)inst * NN : nullptr)) st |= PT_SINGULAR;
     if (tid == 0) {
       for (int q = 0; q < a.nbot; ++q) {
         const int io = N - a.nw + a.bot[q] - 1;
-        const double v = gj_diag(N, s, io).y;
+        const double v = ginv(io, io).y;
         dr = a.divide_by_pi ? dr - v / PI_REF : dr - v;
       }
       if (a.spin[0]) {                                        // src/surfstat.f90:178-192
-        auto gr = [&](int i, int j) { return s.big[i + s.cols[j] * N]; };
         if (a.spin_right_bottom)                              // src/fermiarc.f90:300-327
-          spin_sums(gr, a.nw, a.nbot, a.bot, N - a.nw, a.divide_by_pi, spin[3], spin[4], spin[5]);
+          spin_sums(ginv, a.nw, a.nbot, a.bot, N - a.nw, a.divide_by_pi, spin[3], spin[4], spin[5]);
         else
-          spin_sums(gr, a.nw, a.ntop, a.top, 0, a.divide_by_pi, spin[3], spin[4], spin[5]);
+          spin_sums(ginv, a.nw, a.ntop, a.top, 0, a.divide_by_pi, spin[3], spin[4], spin[5]);
       }
     }
     __syncthreads();
     // GB = (w - eps)^-1                                      // :133-134
-    if (gj_invert(E, w, N, s)) st |= PT_SINGULAR;
-    if (a.gb) gj_store(N, s, a.gb + (size_t)inst * NN);
+    if (invert(E, a.gb ? a.gb + (size_t)inst * NN : nullptr)) st |= PT_SINGULAR;
     if (tid == 0) {
       for (int i = 0; i < N; ++i) {
-        const double v = gj_diag(N, s, i).y;
+        const double v = ginv(i, i).y;
         db = a.divide_by_pi ? db - v / PI_REF : db - v;
       }
       if (!isfinite(dl) || !isfinite(dr) || !isfinite(db)) st |= PT_NONFINITE;
@@ -165,71 +167,87 @@ __global__ void __launch_bounds__(512, 1) k_decimate_fp64(const DecimArgs a) {
   }
 }
 
-// one product C = X*Y (op 0) or inverse C = X^-1 (op 1) in FP64 by one CTA
-__global__ void __launch_bounds__(512, 1) k_fp64_unit(int op, int N, int KC, const double2* X,
-                                                     const double2* Y, double2* C, double2* negX,
+// one product C = X*Y (op 0) or inverse C = X^-1 (op 1) in FP64 by one CTA;
+// gi: the inverse in global memory (work: negX then Mg, N x N each)
+template <bool GI>
+__global__ void __launch_bounds__(GI ? 256 : 512, 1) k_fp64_unit(int op, int N, int KC,
+                                                     const double2* X, const double2* Y,
+                                                     double2* C, double2* negX, double2* Mg,
                                                      int* status) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int NN = N * N;
-  const size_t big = (size_t)max(NN, 2 * N * KC);
-  Shared s;
-  s.big = reinterpret_cast<double2*>(smraw);
-  s.sX = s.big;
-  s.sY = s.big + (size_t)N * KC;
-  s.colbuf = s.big + big;
-  s.rowbuf = s.colbuf + N;
-  s.recip = s.rowbuf + N;
-  s.red = reinterpret_cast<double*>(s.recip + 2);
-  s.perm = reinterpret_cast<int*>(s.red + 32);
-  s.cols = s.perm + N;
-  s.misc = s.cols + N;
+  const Shared s = fp64_layout(smraw, N, KC, !GI);
   if (op == 0) {
     cta_gemm<13, EPI_STORE>(X, Y, N, KC, s.sX, s.sY, C, nullptr);
     if (threadIdx.x == 0) *status = 0;
   } else {
     for (int e = threadIdx.x; e < NN; e += blockDim.x) negX[e] = make_double2(-X[e].x, -X[e].y);
     __syncthreads();
-    const int sing = gj_invert(negX, make_double2(0.0, 0.0), N, s);   // (0 I - (-X))^-1
-    gj_store(N, s, C);
+    int sing;
+    if (GI) {                                                   // (0 I - (-X))^-1
+      sing = gj_invert_global(negX, make_double2(0.0, 0.0), N, Mg, s);
+      gj_store_global(N, Mg, s, C);
+    } else {
+      sing = gj_invert(negX, make_double2(0.0, 0.0), N, s);
+      gj_store(N, s, C);
+    }
     if (threadIdx.x == 0) *status = sing ? PT_SINGULAR : 0;
   }
 }
 
-size_t smem_bytes(int N, int KC) {
-  const size_t big = (size_t)(N * N > 2 * N * KC ? N * N : 2 * N * KC);
-  return big * 16 + (size_t)N * 32 + 32 + 32 * 8 + (size_t)N * 8 + 16;
+size_t smem_bytes(int N, int KC, bool inv_in_smem) {
+  const size_t big = inv_in_smem ? (size_t)(N * N > 2 * N * KC ? N * N : 2 * N * KC)
+                                 : (size_t)2 * N * KC;
+  return big * 16 + (size_t)N * 32 + 16 * GJ_PANEL + 32 * 8 + (size_t)N * 8 + 16;
+}
+
+template <int RP>
+const void* fp64_kernel(bool gi) {
+  return gi ? (const void*)k_decimate_fp64<13, true> : (const void*)k_decimate_fp64<RP, false>;
 }
 
 }  // namespace
 
 int decim_fp64_max_n() {
   int n = 8;
-  while (smem_bytes(n + 1, (n + 1) / 2) <= 227 * 1024) ++n;
+  while (smem_bytes(n + 1, (n + 1) / 2, true) <= 227 * 1024) ++n;
   return n;
 }
 
-cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg) {
+int decim_fp64_large_max_n() { return 32 * GJ_ROWS; }
+
+size_t decim_fp64_ws_matrices(const DecimConfig& cfg) { return cfg.inv_global ? 9 : 8; }
+
+cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg, bool force_global) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   int smem_optin = 0;
   e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
+  const bool gi = force_global || N > decim_fp64_max_n();
+  if (gi && N > decim_fp64_large_max_n()) return cudaErrorInvalidValue;
   int T = threads_override > 0 ? threads_override : (N <= 48 ? 128 : (N <= 80 ? 256 : 512));
   int KC = N;
-  if (smem_bytes(N, KC) > (size_t)smem_optin) KC = (N + 1) / 2;
-  while (KC > 1 && smem_bytes(N, KC) > (size_t)smem_optin) --KC;
+  if (gi) {
+    T = 256;                       // 255 registers: a lane keeps 10 rows of a column
+    KC = 16;
+  } else if (smem_bytes(N, KC, true) > (size_t)smem_optin) {
+    KC = (N + 1) / 2;
+  }
+  while (KC > GJ_PANEL && smem_bytes(N, KC, !gi) > (size_t)smem_optin) --KC;
+  if (smem_bytes(N, KC, !gi) > (size_t)smem_optin) return cudaErrorInvalidValue;
   const int rounds = (N * N + T - 1) / T;
   int RP = 13;
-  if (rounds <= 4) RP = 4;
-  else if (rounds <= 8) RP = 8;
+  if (!gi && rounds <= 4) RP = 4;
+  else if (!gi && rounds <= 8) RP = 8;
   cfg->threads = T;
   cfg->KC = KC;
   cfg->RP = RP;
-  cfg->smem = smem_bytes(N, KC);
+  cfg->inv_global = gi ? 1 : 0;
+  cfg->smem = smem_bytes(N, KC, !gi);
   int occ = 0;
-  const void* fn = RP == 4 ? (const void*)k_decimate_fp64<4>
-                           : (RP == 8 ? (const void*)k_decimate_fp64<8> : (const void*)k_decimate_fp64<13>);
+  const void* fn = RP == 4 ? fp64_kernel<4>(gi) : (RP == 8 ? fp64_kernel<8>(gi) : fp64_kernel<13>(gi));
   e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg->smem);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, T, cfg->smem);
@@ -240,22 +258,31 @@ cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg) {
 
 cudaError_t launch_decimate_fp64(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                  cudaStream_t s) {
+  if (cfg.inv_global) {
+    k_decimate_fp64<13, true><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    return cudaGetLastError();
+  }
   switch (cfg.RP) {
-    case 4: k_decimate_fp64<4><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
-    case 8: k_decimate_fp64<8><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
-    default: k_decimate_fp64<13><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
+    case 4: k_decimate_fp64<4, false><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
+    case 8: k_decimate_fp64<8, false><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
+    default: k_decimate_fp64<13, false><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_fp64_unit(int op, int N, const double2* X, const double2* Y, double2* C,
-                             double2* negX, int* status, cudaStream_t st) {
+                             double2* work, int* status, cudaStream_t st) {
   DecimConfig cfg;
   cudaError_t e = decim_fp64_config(N, 512, &cfg);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_fp64_unit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+  const void* fn = cfg.inv_global ? (const void*)k_fp64_unit<true> : (const void*)k_fp64_unit<false>;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
   if (e != cudaSuccess) return e;
-  k_fp64_unit<<<1, 512, cfg.smem, st>>>(op, N, cfg.KC, X, Y, C, negX, status);
+  double2* mg = work + (size_t)N * N;
+  if (cfg.inv_global)
+    k_fp64_unit<true><<<1, cfg.threads, cfg.smem, st>>>(op, N, cfg.KC, X, Y, C, work, mg, status);
+  else
+    k_fp64_unit<false><<<1, 512, cfg.smem, st>>>(op, N, cfg.KC, X, Y, C, work, mg, status);
   return cudaGetLastError();
 }
 

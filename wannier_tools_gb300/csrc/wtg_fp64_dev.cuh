@@ -78,18 +78,43 @@ __device__ double cta_gemm(const double2* __restrict__ X, const double2* __restr
   return nrm;
 }
 
+constexpr int GJ_PANEL = 8;   // pivot steps per pass of the global-memory Gauss-Jordan
+
 struct Shared {
   double2* big;      // N*N inverse work, or the GEMM stages
   double2* sX;
   double2* sY;
+  double2* pan;      // [N][GJ_PANEL] panel columns (global-memory inverse; aliases the stages)
+  double2* mult;     // [N][GJ_PANEL] elimination multipliers of the panel's steps (same)
   double2* colbuf;   // [N]
   double2* rowbuf;   // [N]
-  double2* recip;    // [2]
+  double2* recip;    // [GJ_PANEL] pivot reciprocals
   double* red;       // [32]
   int* perm;         // [N]
   int* cols;         // [N]
   int* misc;         // [4]: 0 instance, 1 singular flag
 };
+
+// Shared-memory layout: the first region holds either the N x N inverse (when
+// it runs in shared memory) or the two GEMM stages of N x KC; the small arrays
+// follow.  fp64_smem_bytes on the host gives the same size.
+__device__ __forceinline__ Shared fp64_layout(unsigned char* smraw, int N, int KC, bool inv_in_smem) {
+  const size_t big = inv_in_smem ? (size_t)max(N * N, 2 * N * KC) : (size_t)2 * N * KC;
+  Shared s;
+  s.big = reinterpret_cast<double2*>(smraw);
+  s.sX = s.big;
+  s.sY = s.big + (size_t)N * KC;
+  s.pan = s.big;
+  s.mult = s.big + (size_t)N * GJ_PANEL;
+  s.colbuf = s.big + big;
+  s.rowbuf = s.colbuf + N;
+  s.recip = s.rowbuf + N;
+  s.red = reinterpret_cast<double*>(s.recip + GJ_PANEL);
+  s.perm = reinterpret_cast<int*>(s.red + 32);
+  s.cols = s.perm + N;
+  s.misc = s.cols + N;
+  return s;
+}
 
 // |re| + |im| (LAPACK's dcabs1, the izamax criterion) as an order-preserving
 // integer key: non-negative doubles compare like their bit patterns.
@@ -191,6 +216,184 @@ __device__ int gj_invert(const double2* __restrict__ X, double2 w, int N, const 
   }
   __syncthreads();
   return singular;
+}
+
+constexpr int GJ_ROWS = 10;    // rows per lane of the global-memory inverse: Ndim <= 320
+
+// one complex entry of a lane's register column (row = lane + 32 m) by a
+// warp-uniform slot index, without local memory
+__device__ __forceinline__ double2 gj_pick(const double2 (&x)[GJ_ROWS], int m) {
+  double2 v = x[0];
+#pragma unroll
+  for (int q = 1; q < GJ_ROWS; ++q)
+    if (q == m) v = x[q];
+  return v;
+}
+
+__device__ __forceinline__ double2 shfl_c(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// Mg := (w I - X)^-1 by the Gauss-Jordan steps of gj_invert, with the matrix
+// in global memory (Ndim too large for shared memory).  The steps run in
+// panels of GJ_PANEL columns: a panel is reduced in shared memory, recording
+// each step's pivot row, reciprocal and multiplier column; then every other
+// column is read once into registers (one warp per column, lane l holding
+// rows l, l+32, ...), put through the panel's steps in order and written
+// back.  Every entry sees the same operations in the same order as in
+// gj_invert, so the two agree bit for bit; global traffic is two N x N sweeps
+// per panel instead of per step.  The inverse is left with permuted columns
+// (inverse(i, j) = Mg[i + cols[j]*N]); an exact zero pivot leaves the
+// identity and returns 1.
+__device__ int gj_invert_global(const double2* __restrict__ X, double2 w, int N,
+                                double2* __restrict__ Mg, const Shared& s) {
+  const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
+  double2* __restrict__ P = s.pan;
+  double2* __restrict__ Cm = s.mult;
+  for (int e = tid; e < NN; e += T) {
+    const double2 x = X[e];
+    double2 v = make_double2(-x.x, -x.y);
+    if (e % (N + 1) == 0) v = make_double2(w.x - x.x, w.y - x.y);
+    Mg[e] = v;
+  }
+  if (tid == 0) s.misc[1] = 0;
+  __syncthreads();
+  for (int k0 = 0; k0 < N; k0 += GJ_PANEL) {
+    const int pb = min(GJ_PANEL, N - k0);
+    for (int e = tid; e < N * pb; e += T) P[e] = Mg[(size_t)k0 * N + e];   // panel columns
+    __syncthreads();
+    for (int t = 0; t < pb; ++t) {
+      const int k = k0 + t;
+      if (warp == 0) {
+        long long best = -1;
+        int bi = N;
+        for (int i = k + lane; i < N; i += 32) {
+          const long long v = cabs1_key(P[i + t * N]);
+          if (v > best) {
+            best = v;
+            bi = i;
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+          }
+        }
+        const int p = bi;
+        for (int i = lane; i < N; i += 32) Cm[i + t * N] = P[(i == p ? k : i) + t * N];
+        if (lane == 0) {
+          s.perm[k] = p;
+          if (best == 0) {
+            s.misc[1] = 1;
+          } else {
+            const double2 pv = P[p + t * N];
+            const double inv_d = 1.0 / (pv.x * pv.x + pv.y * pv.y);
+            s.recip[t] = make_double2(pv.x * inv_d, -pv.y * inv_d);
+          }
+        }
+      }
+      __syncthreads();
+      if (s.misc[1]) break;
+      const int p = s.perm[k];
+      const double2 r = s.recip[t];
+      if (tid < pb) {                       // pivot row of the panel
+        const int j = tid;
+        const double2 akj = P[k + j * N];
+        const double2 apj = P[p + j * N];
+        if (p != k) P[p + j * N] = akj;
+        const double2 nk = (j == t) ? r : cmul(apj, r);
+        P[k + j * N] = nk;
+        s.rowbuf[j] = nk;
+      }
+      __syncthreads();
+      for (int e = tid; e < N * pb; e += T) {
+        const int i = e % N, j = e / N;
+        if (i != k) {
+          double2 v = (j == t) ? make_double2(0.0, 0.0) : P[e];
+          const double2 f = Cm[i + t * N];
+          const double2 rk = s.rowbuf[j];
+          v.x = fma(-f.x, rk.x, v.x);
+          v.x = fma(f.y, rk.y, v.x);
+          v.y = fma(-f.x, rk.y, v.y);
+          v.y = fma(-f.y, rk.x, v.y);
+          P[e] = v;
+        }
+      }
+      __syncthreads();
+    }
+    if (s.misc[1]) break;
+    // every column outside the panel through the panel's steps, in registers
+    for (int j = warp; j < N; j += nwarp) {
+      if (j >= k0 && j < k0 + pb) continue;
+      double2* col = Mg + (size_t)j * N;
+      double2 x[GJ_ROWS];
+#pragma unroll
+      for (int q = 0; q < GJ_ROWS; ++q) {
+        const int i = lane + 32 * q;
+        x[q] = i < N ? col[i] : make_double2(0.0, 0.0);
+      }
+      for (int t = 0; t < pb; ++t) {
+        const int k = k0 + t, p = s.perm[k];
+        const double2 r = s.recip[t];
+        const double2 akj = shfl_c(gj_pick(x, k >> 5), k & 31);
+        const double2 apj = shfl_c(gj_pick(x, p >> 5), p & 31);
+        const double2 nk = cmul(apj, r);
+        const double2* cm = Cm + t * N;
+#pragma unroll
+        for (int q = 0; q < GJ_ROWS; ++q) {
+          const int i = lane + 32 * q;
+          if (i < N && i != k) {
+            double2 v = (i == p) ? akj : x[q];
+            const double2 f = cm[i];
+            v.x = fma(-f.x, nk.x, v.x);
+            v.x = fma(f.y, nk.y, v.x);
+            v.y = fma(-f.x, nk.y, v.y);
+            v.y = fma(-f.y, nk.x, v.y);
+            x[q] = v;
+          } else if (i == k) {
+            x[q] = nk;
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < GJ_ROWS; ++q) {
+        const int i = lane + 32 * q;
+        if (i < N) col[i] = x[q];
+      }
+    }
+    for (int e = tid; e < N * pb; e += T) Mg[(size_t)k0 * N + e] = P[e];
+    __syncthreads();
+  }
+  const int singular = s.misc[1];
+  if (singular) {
+    for (int e = tid; e < NN; e += T) Mg[e] = make_double2(e % (N + 1) == 0 ? 1.0 : 0.0, 0.0);
+    for (int j = tid; j < N; j += T) s.cols[j] = j;
+  } else if (tid == 0) {
+    for (int j = 0; j < N; ++j) s.cols[j] = j;
+    for (int k = N - 1; k >= 0; --k) {
+      const int p = s.perm[k];
+      const int t = s.cols[k];
+      s.cols[k] = s.cols[p];
+      s.cols[p] = t;
+    }
+  }
+  __syncthreads();
+  return singular;
+}
+
+// out = the un-permuted inverse left in Mg by gj_invert_global
+__device__ void gj_store_global(int N, const double2* __restrict__ Mg, const Shared& s,
+                                double2* __restrict__ out) {
+  const int T = blockDim.x, NN = N * N;
+  for (int e = threadIdx.x; e < NN; e += T) {
+    const int i = e % N, j = e / N;
+    out[e] = Mg[i + (size_t)s.cols[j] * N];
+  }
 }
 
 // write the un-permuted inverse from shared memory to global
