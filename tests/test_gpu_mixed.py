@@ -27,13 +27,12 @@ def nrel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("n", [1, 8, 17, 40, 64, 112])
+@pytest.mark.parametrize("n", [1, 8, 17, 40, 64, 112, 130, 200, 257, 320])
 def test_mat_mul_both_precisions(built_lib, n):
     rng = np.random.default_rng(n)
     a, b = crand(rng, n), crand(rng, n)
     ref = a @ b
-    if n <= 119:                      # the FP64 kernel's shared-memory limit
-        assert nrel(api.mat_mul(a, b, PREC_FP64), ref) <= 1e-14
+    assert nrel(api.mat_mul(a, b, PREC_FP64), ref) <= 1e-14
     assert nrel(api.mat_mul(a, b, PREC_MIXED), ref) <= 1e-10
 
 
@@ -52,14 +51,13 @@ def test_mat_mul_mixed_wide_dynamic_range(built_lib):
     assert np.max(np.abs(got - ref) / scale) <= 1e-10
 
 
-@pytest.mark.parametrize("n", [1, 5, 40, 112])
+@pytest.mark.parametrize("n", [1, 5, 40, 112, 113, 200, 264, 320])
 def test_inverse_both_precisions(built_lib, n):
     rng = np.random.default_rng(100 + n)
     a = crand(rng, n) + 3.0 * np.sqrt(n) * np.eye(n)
     ref = np.linalg.inv(a)
-    if n <= 119:
-        g64, st64 = api.inv(a, PREC_FP64)
-        assert st64 == 0 and nrel(g64, ref) <= 1e-13
+    g64, st64 = api.inv(a, PREC_FP64)
+    assert st64 == 0 and nrel(g64, ref) <= 1e-13
     gmx, stmx = api.inv(a, PREC_MIXED)
     assert stmx == 0 and nrel(gmx, ref) <= 1e-9
 
@@ -85,20 +83,16 @@ def _rel(a, b):
     (20, 2, 1e-2, [-0.6, 0.0, 0.45], False),    # surfstat shape, Ndim 40
     (56, 2, 1e-3, [0.0], True),                  # Fermi-arc shape, Ndim 112
     (8, 2, 1e-4, [0.0, 0.7], False),             # small eta, Ndim 16
-    (44, 3, 1e-3, [0.05], False),                # Np = 3, Ndim 132 > 112: rejected
+    (44, 3, 1e-3, [0.05], False),                # Np = 3, Ndim 132: two row blocks
+    (88, 3, 1e-3, [-0.2], False),                # Ndim 264: six accumulators, three row blocks
 ])
 def test_spectrum_mixed_vs_fp64_oracle(built_lib, nw, np_, eta_ev, oms, arc):
-    from wannier_tools_gb300._lib import WtgError
     m = synthetic.make_model(nw, np_, seed=nw + np_)
-    kp = synthetic.random_kpoints(3, seed=nw)
+    kp = synthetic.random_kpoints(3 if nw * np_ <= 132 else 2, seed=nw)
     om = np.asarray(oms) * EV
     top = list(range(1, nw + 1, 2))
     bot = list(range(2, nw + 1, 3))
     with api.Model.from_surface_model(m) as g:
-        if nw * np_ > 112:
-            with pytest.raises(WtgError):
-                g.surface_spectrum(kp, om, eta_ev * EV, top, bot, precision=PREC_MIXED)
-            return
         got = g.surface_spectrum(kp, om, eta_ev * EV, top, bot, divide_by_pi=arc,
                                  precision=PREC_MIXED)
     ref = O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, nw, np_, kp, om, eta_ev * EV, top, bot,
@@ -109,6 +103,14 @@ def test_spectrum_mixed_vs_fp64_oracle(built_lib, nw, np_, eta_ev, oms, arc):
         assert e <= 1e-5, (name, e)
     assert np.abs(got["iters"] - ref["iters"]).max() <= 1
     assert (got["status"] == 0).all()
+
+
+def test_mixed_ndim_limit(built_lib):
+    from wannier_tools_gb300._lib import WtgError
+    m = synthetic.make_model(161, 2, seed=3)
+    with api.Model.from_surface_model(m) as g:
+        with pytest.raises(WtgError):
+            g.surface_spectrum([[0.3, 0.3]], [0.0], 1e-2, [1], [1], precision=PREC_MIXED)
 
 
 def test_spin_mixed(built_lib):

@@ -52,6 +52,42 @@ constexpr unsigned SPIN_LIMIT = 1u << 22;
 constexpr int PT_TIMEOUT = 8;
 
 constexpr int OZ_STORE = 0, OZ_ADD2 = 1, OZ_STORE_NORM = 2, OZ_IMINUS = 3, OZ_ADDTO = 4;
+constexpr int MX_MAXN = 320;         // largest Ndim
+constexpr int MX_SMEM_GJ_N = 112;    // up to here the FP32 Gauss-Jordan runs in shared memory
+constexpr int MX_PANEL = 16;         // pivot steps per panel of the global-memory Gauss-Jordan
+constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident column
+
+// How one product is cut into tensor-memory passes.  Rows go in blocks of
+// M = 128.  Each pass holds nacc FP32 accumulators of w columns for one
+// component (or both components when they fit: both = 1), so 512 tensor-memory
+// columns bound nacc * w; output columns [0, NP) go in ncb blocks of w0 (the
+// last block narrower).  nacc = 5 keeps slice orders 2..5 exact for K <= 256;
+// above that order 5 is split over two K halves (nacc = 6), since 4 * 127^2 * K
+// must stay below 2^24.
+struct MxPlan {
+  int N, NP, nrb, nacc, both, ncb, w0;
+};
+
+__host__ __device__ inline MxPlan mx_plan(int N) {
+  MxPlan p;
+  p.N = N;
+  p.NP = (N + 15) & ~15;
+  p.nrb = (N + 127) / 128;
+  p.nacc = N > 256 ? 6 : 5;
+  p.both = 2 * p.nacc * p.NP <= 512 ? 1 : 0;
+  if (p.both) {
+    p.ncb = 1;
+    p.w0 = p.NP;
+  } else {
+    p.ncb = (p.nacc * p.NP + 511) / 512;
+    for (;;) {
+      p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 15) & ~15;
+      if (p.nacc * p.w0 <= 512) break;
+      ++p.ncb;
+    }
+  }
+  return p;
+}
 
 __device__ __forceinline__ uint32_t saddr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -194,6 +230,8 @@ __device__ __forceinline__ double f2d_bits(float f) {     // exact FP32 -> FP64
 struct MxShared {
   unsigned char* buf[2];   // per buffer: 2*NSL A planes then 2*NSL B planes
   float2* gj;              // FP32 Gauss-Jordan matrix (aliases the buffers)
+  float2* pan;             // [N][MX_PANEL] panel of the global-memory Gauss-Jordan (aliases)
+  float2* mult;            // [N][MX_PANEL] its multiplier columns (aliases)
   float2* colbuf;
   float2* rowbuf;
   float2* recip;
@@ -209,29 +247,29 @@ struct MxShared {
   uint16_t* lutB;          // [NSL][128] BF16 bits of d * 2^(7(5-q))
 };
 
-constexpr int NACC = 5;              // accumulators per pass: t = 2, 3, 4, 5 exact; t >= 6
-
-__device__ __forceinline__ int bufbytes_of(int NP) {
-  return 2 * NSL * APLANE + 2 * NSL * NP * KCH * 2;
+__host__ __device__ __forceinline__ int bufbytes_of(int WB) {
+  return 2 * NSL * APLANE + 2 * NSL * WB * KCH * 2;
 }
 
 // shared-memory layout: two operand buffers (the FP32 Gauss-Jordan matrix
 // aliases them), then the small arrays
-__device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int NP) {
+__device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int N, int WB) {
   MxShared s;
-  const int bb = bufbytes_of(NP);
+  const int bb = bufbytes_of(WB);
   s.buf[0] = smraw;
   s.buf[1] = smraw + bb;
   s.gj = reinterpret_cast<float2*>(smraw);
+  s.pan = reinterpret_cast<float2*>(smraw);
+  s.mult = s.pan + (size_t)N * MX_PANEL;
   unsigned char* tail = smraw + 2 * bb;
   s.colbuf = reinterpret_cast<float2*>(tail);
-  s.rowbuf = s.colbuf + 128;
-  s.recip = s.rowbuf + 128;
-  s.perm = reinterpret_cast<int*>(s.recip + 2);
-  s.cols = s.perm + 128;
-  s.expA = s.cols + 128;
-  s.expB = s.expA + 128;
-  s.red = reinterpret_cast<float*>(s.expB + 128);
+  s.rowbuf = s.colbuf + MX_MAXN;
+  s.recip = s.rowbuf + MX_MAXN;
+  s.perm = reinterpret_cast<int*>(s.recip + MX_PANEL);
+  s.cols = s.perm + MX_MAXN;
+  s.expA = s.cols + MX_MAXN;
+  s.expB = s.expA + MX_MAXN;
+  s.red = reinterpret_cast<float*>(s.expB + MX_MAXN);
   s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
   s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
   s.misc = reinterpret_cast<int*>(s.tslot + 2);
@@ -269,13 +307,15 @@ __device__ __forceinline__ void mx_fill_luts(const MxShared& s) {
 __device__ void oz_exponents(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
                              MxShared& s) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int r = threadIdx.x; r < 128; r += blockDim.x) s.expA[r] = 0;
+  for (int r = threadIdx.x; r < MX_MAXN; r += blockDim.x) s.expA[r] = 0;
   __syncthreads();
-  int rmax[4] = {0, 0, 0, 0};
+  int rmax[MX_ROWS];
+#pragma unroll
+  for (int m = 0; m < MX_ROWS; ++m) rmax[m] = 0;
   for (int k = warp; k < N; k += nwarp) {
     const double2* xc = X + (size_t)k * N;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < MX_ROWS; ++m) {
       const int i = lane + 32 * m;
       if (i < N) {
         const double2 v = xc[i];
@@ -284,7 +324,7 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
     }
   }
 #pragma unroll
-  for (int m = 0; m < 4; ++m)
+  for (int m = 0; m < MX_ROWS; ++m)
     if (lane + 32 * m < N) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
   for (int j = warp; j < N; j += nwarp) {
     const double2* yc = Y + (size_t)j * N;
@@ -308,18 +348,18 @@ __device__ __forceinline__ uint32_t dig2(const uint16_t* lut, unsigned long long
 }
 
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                            int NP, int k0, int jb, int width, const MxShared& s, int b) {
+                            int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b) {
   unsigned char* __restrict__ A = s.buf[b];
   unsigned char* __restrict__ B = A + 2 * NSL * APLANE;
   const int* __restrict__ expA = s.expA;
   const int* __restrict__ expB = s.expB;
   const uint16_t* __restrict__ lutA = s.lutA;
   const uint16_t* __restrict__ lutB = s.lutB;
-  const int bplane = NP * KCH * 2;
+  const int bplane = WB * KCH * 2;
   for (int it = threadIdx.x; it < 128 * (KCH / 2); it += blockDim.x) {
-    const int i = it & 127, kk = 2 * (it >> 7);
+    const int il = it & 127, kk = 2 * (it >> 7), i = rb0 + il;
     if (i >= N) {                                  // padding rows of the M = 128 tile
-      const int off = (((i >> 3) * 2 + (kk >> 3)) * 64 + (i & 7) * 8 + (kk & 7)) * 2;
+      const int off = (((il >> 3) * 2 + (kk >> 3)) * 64 + (il & 7) * 8 + (kk & 7)) * 2;
 #pragma unroll
       for (int pl = 0; pl < 2 * NSL; ++pl) *reinterpret_cast<uint32_t*>(A + pl * APLANE + off) = 0u;
       continue;
@@ -334,7 +374,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(x0.x, E, n0r), f0i = fixed49(x0.y, E, n0i);
     const unsigned long long f1r = fixed49(x1.x, E, n1r), f1i = fixed49(x1.y, E, n1i);
-    const int off = (((i >> 3) * 2 + (kk >> 3)) * 64 + (i & 7) * 8 + (kk & 7)) * 2;
+    const int off = (((il >> 3) * 2 + (kk >> 3)) * 64 + (il & 7) * 8 + (kk & 7)) * 2;
 #pragma unroll
     for (int p = 1; p <= NSL; ++p) {
       const int sh = 7 * (NSL - p);
@@ -374,16 +414,18 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 
 // all slice-pair MMAs of one chunk (thread 0 only).  The descriptors' start
 // address field holds (address >> 4) in its low 14 bits, so a plane offset is
-// added to a base descriptor directly.  Accumulator a = min(t, 6) - 2 sits at
-// tensor-memory column a * width.
-__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int width, int comp,
-                         bool first, uint32_t bank) {
+// added to a base descriptor directly.  Slice order t = p + q goes to
+// accumulator t - 2 for t <= 5 (with nacc = 6, order 5 of the second K half to
+// accumulator 4) and to the last accumulator for t >= 6; accumulator a sits at
+// tensor-memory column bank + a * width.  amask holds the accumulators already
+// written in this pass (bit abase + a): the first MMA into one overwrites.
+__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int WB, int width, int comp,
+                         uint32_t bank, int nacc, int khalf, uint32_t& amask, int abase) {
   const uint32_t A = saddr(s.buf[b]);
   const uint32_t B = A + 2 * NSL * APLANE;
-  const uint64_t bplane16 = (uint64_t)NP * KCH * 2 >> 4;
+  const uint64_t bplane16 = (uint64_t)WB * KCH * 2 >> 4;
   const uint64_t adesc0 = sdesc(A), bdesc0 = sdesc(B);
   const uint32_t id_pos = idesc(width, 0), id_neg = idesc(width, 1);
-  unsigned started = 0u;
 #pragma unroll 1
   for (int p = 1; p <= NSL; ++p) {
     const uint64_t aR = adesc0 + (uint64_t)(2 * (p - 1)) * (APLANE >> 4);
@@ -391,12 +433,13 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int wi
 #pragma unroll 1
     for (int q = 1; q + p <= NSL + 1; ++q) {
       const int t = p + q;
-      const int a = t <= 5 ? t - 2 : 4;
+      const int a = t <= 4 ? t - 2 : (t == 5 ? 3 + khalf : nacc - 1);
       const uint32_t d = tmem + bank + (uint32_t)(a * width);
       const uint64_t bR = bdesc0 + (uint64_t)(2 * (q - 1)) * bplane16;
       const uint64_t bI = bR + bplane16;
-      const uint32_t acc = (first && !((started >> a) & 1u)) ? 0u : 1u;
-      started |= 1u << a;
+      const uint32_t bit = 1u << (abase + a);
+      const uint32_t acc = (amask & bit) ? 1u : 0u;
+      amask |= bit;
       if (comp == 0) {          // Cr = Xr Yr - Xi Yi
         mma_bf16(d, aR, bR, id_pos, acc);
         mma_bf16(d, aI, bI, id_neg, 1u);
@@ -409,127 +452,130 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int NP, int wi
 }
 
 // C = X * Y through the epilogue; returns this thread's FP32 partial of sum |C|
-// (OZ_STORE_NORM only).  out0/out1/src: FP64 N x N column-major.
+// (OZ_STORE_NORM, OZ_IMINUS).  out0/out1/src: FP64 N x N column-major.
 template <int EPI>
-__device__ float oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                         int NP, double2* out0, double2* out1, const double2* src, MxShared& s,
-                         MxState& st) {
-  const int tid = threadIdx.x;
+__device__ float oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y,
+                         const MxPlan& pl, double2* out0, double2* out1, const double2* src,
+                         MxShared& s, MxState& st) {
+  const int N = pl.N, tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
-  // both components in one pass when their accumulators fit tensor memory
-  // (Ndim <= 48), else one component per pass over one or two column halves
-  const bool both = 2 * NACC * NP <= 512;
-  const int nsplit = NACC * NP <= 512 ? 1 : 2;
-  const int w0 = nsplit == 1 ? NP : ((NP / 2 + 15) & ~15);
-  const int npass = both ? 1 : 2 * nsplit;
+  const int nacc = pl.nacc, WB = pl.w0;
+  const int npass = pl.both ? 1 : 2 * pl.ncb;
   float nrm = 0.f;
   oz_exponents(X, Y, N, s);
   __syncthreads();
-  for (int pass = 0; pass < npass && !st.abort; ++pass) {
-    const int comp0 = both ? 0 : pass / nsplit, comp1 = both ? 1 : comp0;
-    const int half = both ? 0 : pass % nsplit;
-    const int jb = half == 0 ? 0 : w0;
-    const int width = nsplit == 1 ? NP : (half == 0 ? w0 : NP - w0);
-    for (int c = 0; c < nch; ++c) {
-      const int b = c & 1;
-      buffer_ready(s, st, b);
-      oz_generate(X, Y, N, NP, c * KCH, jb, width, s, b);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tc_fence_before();
+  for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
+    const int rb0 = rb * 128;
+    for (int pass = 0; pass < npass && !st.abort; ++pass) {
+      const int comp0 = pl.both ? 0 : pass / pl.ncb, comp1 = pl.both ? 1 : comp0;
+      const int cbi = pl.both ? 0 : pass % pl.ncb;
+      const int jb = cbi * pl.w0;
+      const int width = min(pl.w0, pl.NP - jb);
+      uint32_t amask = 0u;
+      for (int c = 0; c < nch; ++c) {
+        const int b = c & 1;
+        buffer_ready(s, st, b);
+        oz_generate(X, Y, N, WB, c * KCH, rb0, jb, width, s, b);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        st.abort = __syncthreads_or(st.abort);
+        tc_fence_after();
+        if (st.abort) break;
+        if (tid == 0) {
+          const int khalf = (nacc == 6 && 2 * c >= nch) ? 1 : 0;
+          for (int comp = comp0; comp <= comp1; ++comp)
+            oz_issue(s, st.tmem, b, WB, width, comp, (uint32_t)((comp - comp0) * nacc * width),
+                     nacc, khalf, amask, 8 * (comp - comp0));
+          mma_commit(&s.mbar[b]);
+        }
+        st.ncommit[b] += 1;
+      }
+      // all MMAs of this pass: the last commit covers every earlier one
+      const int bl = (nch - 1) & 1;
+      if (!st.abort && !mbar_wait(&s.mbar[bl], (st.ncommit[bl] - 1) & 1)) st.abort = 1;
+      if (!st.abort) {
+        st.nwaited[0] = st.ncommit[0];
+        st.nwaited[1] = st.ncommit[1];
+      }
       st.abort = __syncthreads_or(st.abort);
       tc_fence_after();
-      if (st.abort) break;
-      if (tid == 0) {
-        for (int comp = comp0; comp <= comp1; ++comp)
-          oz_issue(s, st.tmem, b, NP, width, comp, c == 0,
-                   (uint32_t)((comp - comp0) * NACC * width));
-        mma_commit(&s.mbar[b]);
-      }
-      st.ncommit[b] += 1;
-    }
-    // all MMAs of this pass: the last commit covers every earlier one
-    const int bl = (nch - 1) & 1;
-    if (!st.abort && !mbar_wait(&s.mbar[bl], (st.ncommit[bl] - 1) & 1)) st.abort = 1;
-    if (!st.abort) {
-      st.nwaited[0] = st.ncommit[0];
-      st.nwaited[1] = st.ncommit[1];
-    }
-    st.abort = __syncthreads_or(st.abort);
-    tc_fence_after();
-    const int* __restrict__ expB = s.expB;
-    for (int comp = comp0; comp <= comp1 && !st.abort; ++comp) {
-      const int warp = tid >> 5, lane = tid & 31;
-      const int quad = warp & 3, hw = warp >> 2;
-      const int row = quad * 32 + lane;
-      const int cb = hw * (width / 2), ce = cb + width / 2;
-      const int er = row < N ? s.expA[row] : 0;
-      const uint32_t bank = (uint32_t)((comp - comp0) * NACC * width);
-      for (int c0 = cb; c0 < ce; c0 += 8) {
-        uint32_t v[NACC][8];
-        const uint32_t ta = st.tmem + bank + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
+      const int* __restrict__ expB = s.expB;
+      for (int comp = comp0; comp <= comp1 && !st.abort; ++comp) {
+        const int warp = tid >> 5, lane = tid & 31;
+        const int quad = warp & 3, hw = warp >> 2;
+        const int row = rb0 + quad * 32 + lane;
+        const int cb = hw * (width / 2), ce = cb + width / 2;
+        const int er = row < N ? s.expA[row] : 0;
+        const uint32_t bank = (uint32_t)((comp - comp0) * nacc * width);
+        for (int c0 = cb; c0 < ce; c0 += 8) {
+          uint32_t v[6][8];
+          const uint32_t ta = st.tmem + bank + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
 #pragma unroll
-        for (int a = 0; a < NACC; ++a) tmem_ld8(ta + (uint32_t)(a * width), v[a]);
-        tmem_wait_ld();
-        if (row < N) {
-          double old0[8], old1[8];
+          for (int a = 0; a < 6; ++a)
+            if (a < nacc) tmem_ld8(ta + (uint32_t)(a * width), v[a]);
+          tmem_wait_ld();
+          if (row < N) {
+            double old0[8], old1[8];
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {            // the epilogue's loads first
-            const int j = jb + c0 + jj;
-            const size_t idx = (size_t)row + (size_t)j * N;
-            old0[jj] = 0.0;
-            old1[jj] = 0.0;
-            if (j < N) {
-              if (EPI == OZ_ADD2) {
-                old0[jj] = reinterpret_cast<const double*>(out0 + idx)[comp];
-                old1[jj] = reinterpret_cast<const double*>(out1 + idx)[comp];
-              } else if (EPI == OZ_ADDTO) {
-                old0[jj] = reinterpret_cast<const double*>(src + idx)[comp];
-              } else if ((EPI == OZ_STORE_NORM || EPI == OZ_IMINUS) && comp == 1) {
-                old0[jj] = out0[idx].x;
+            for (int jj = 0; jj < 8; ++jj) {            // the epilogue's loads first
+              const int j = jb + c0 + jj;
+              const size_t idx = (size_t)row + (size_t)j * N;
+              old0[jj] = 0.0;
+              old1[jj] = 0.0;
+              if (j < N) {
+                if (EPI == OZ_ADD2) {
+                  old0[jj] = reinterpret_cast<const double*>(out0 + idx)[comp];
+                  old1[jj] = reinterpret_cast<const double*>(out1 + idx)[comp];
+                } else if (EPI == OZ_ADDTO) {
+                  old0[jj] = reinterpret_cast<const double*>(src + idx)[comp];
+                } else if ((EPI == OZ_STORE_NORM || EPI == OZ_IMINUS) && comp == 1) {
+                  old0[jj] = out0[idx].x;
+                }
               }
             }
-          }
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const int j = jb + c0 + jj;
-            if (j < N) {
-              long long S = 0;
+            for (int jj = 0; jj < 8; ++jj) {
+              const int j = jb + c0 + jj;
+              if (j < N) {
+                long long S = 0;
 #pragma unroll
-              for (int a = 0; a < NACC; ++a) S += f2ll_int(v[a][jj]);
-              const double val = assemble(S, er + expB[j] - 1070);
-              const size_t idx = (size_t)row + (size_t)j * N;
-              double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
-              if (EPI == OZ_STORE) {
-                *o0 = val;
-              } else if (EPI == OZ_ADD2) {
-                *o0 = old0[jj] + val;
-                *(reinterpret_cast<double*>(out1 + idx) + comp) = old1[jj] + val;
-              } else if (EPI == OZ_STORE_NORM) {
-                *o0 = val;
-                if (comp == 1) {
-                  const float re = fabsf(d2f_bits(old0[jj])), im = fabsf(d2f_bits(val));
-                  const float hi = fmaxf(re, im), lo = fminf(re, im);
-                  if (hi > 0.f) {
-                    const float r = lo / hi;
-                    nrm += hi * sqrtf(fmaf(r, r, 1.f));
+                for (int a = 0; a < 6; ++a)
+                  if (a < nacc) S += f2ll_int(v[a][jj]);
+                const double val = assemble(S, er + expB[j] - 1070);
+                const size_t idx = (size_t)row + (size_t)j * N;
+                double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
+                if (EPI == OZ_STORE) {
+                  *o0 = val;
+                } else if (EPI == OZ_ADD2) {
+                  *o0 = old0[jj] + val;
+                  *(reinterpret_cast<double*>(out1 + idx) + comp) = old1[jj] + val;
+                } else if (EPI == OZ_STORE_NORM) {
+                  *o0 = val;
+                  if (comp == 1) {
+                    const float re = fabsf(d2f_bits(old0[jj])), im = fabsf(d2f_bits(val));
+                    const float hi = fmaxf(re, im), lo = fminf(re, im);
+                    if (hi > 0.f) {
+                      const float r = lo / hi;
+                      nrm += hi * sqrtf(fmaf(r, r, 1.f));
+                    }
                   }
+                } else if (EPI == OZ_IMINUS) {
+                  double w = -val;
+                  if (comp == 0 && row == j) w += 1.0;
+                  *o0 = w;
+                  if (comp == 1) nrm += fabsf(d2f_bits(old0[jj])) + fabsf(d2f_bits(w));
+                } else {   // OZ_ADDTO
+                  *o0 = old0[jj] + val;
                 }
-              } else if (EPI == OZ_IMINUS) {
-                double w = -val;
-                if (comp == 0 && row == j) w += 1.0;
-                *o0 = w;
-                if (comp == 1) nrm += fabsf(d2f_bits(old0[jj])) + fabsf(d2f_bits(w));
-              } else {   // OZ_ADDTO
-                *o0 = old0[jj] + val;
               }
             }
           }
         }
       }
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
     }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
   }
   return nrm;
 }
@@ -685,20 +731,205 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
 }
 
 
+__device__ __forceinline__ float2 pick_f(const float2 (&x)[MX_ROWS], int m) {
+  float2 v = x[0];
+#pragma unroll
+  for (int q = 1; q < MX_ROWS; ++q)
+    if (q == m) v = x[q];
+  return v;
+}
+
+__device__ __forceinline__ float2 shfl_f2(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// As gj32_start for Ndim above the shared-memory limit: the FP32 matrix lives
+// in global memory (Wf, N x N float2) and the pivot steps run in panels of
+// MX_PANEL columns.  A panel is reduced in shared memory (pivot rows,
+// reciprocals and multiplier columns recorded); then each other column is read
+// once into registers (one warp per column, lane l holding rows l, l+32, ...),
+// put through the panel's steps in order and written back.  Same operations
+// per entry as gj32_start.
+__device__ int gj32_global(const double2* __restrict__ X, double2 w, int N, double2* Mi,
+                           double2* G, float2* __restrict__ Wf, MxShared& s_) {
+  const int T = blockDim.x, tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
+  float2* __restrict__ P = s_.pan;
+  float2* __restrict__ Cm = s_.mult;
+  float2* __restrict__ rowbuf = s_.rowbuf;
+  float2* __restrict__ recip = s_.recip;
+  int* __restrict__ perm = s_.perm;
+  int* __restrict__ cols = s_.cols;
+  int* __restrict__ misc = s_.misc;
+  for (int j = warp; j < N; j += nwarp) {
+    for (int i = lane; i < N; i += 32) {
+      const size_t e = (size_t)i + (size_t)j * N;
+      const double2 x = X[e];
+      double2 m = make_double2(-x.x, -x.y);
+      if (i == j) m = make_double2(w.x - x.x, w.y - x.y);
+      Mi[e] = m;
+      Wf[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+    }
+  }
+  if (tid == 0) misc[1] = 0;
+  __syncthreads();
+  for (int k0 = 0; k0 < N; k0 += MX_PANEL) {
+    const int pb = min(MX_PANEL, N - k0);
+    for (int e = tid; e < N * pb; e += T) P[e] = Wf[(size_t)k0 * N + e];
+    __syncthreads();
+    for (int t = 0; t < pb; ++t) {
+      const int k = k0 + t;
+      if (warp == 0) {
+        long long best = -1;
+        int bi = N;
+        for (int i = k + lane; i < N; i += 32) {
+          const long long v = cabs1_key_f(P[i + t * N]);
+          if (v > best) {
+            best = v;
+            bi = i;
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+          }
+        }
+        const int p = bi;
+        for (int i = lane; i < N; i += 32) Cm[i + t * N] = P[(i == p ? k : i) + t * N];
+        if (lane == 0) {
+          perm[k] = p;
+          if (best == 0) {
+            misc[1] = 1;
+          } else {
+            const float2 pv = P[p + t * N];
+            const float inv_d = 1.0f / (pv.x * pv.x + pv.y * pv.y);
+            recip[t] = make_float2(pv.x * inv_d, -pv.y * inv_d);
+          }
+        }
+      }
+      __syncthreads();
+      if (misc[1]) break;
+      const int p = perm[k];
+      const float2 r = recip[t];
+      if (tid < pb) {
+        const int j = tid;
+        const float2 akj = P[k + j * N];
+        const float2 apj = P[p + j * N];
+        if (p != k) P[p + j * N] = akj;
+        const float2 nk = (j == t) ? r
+                                   : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
+                                                 fmaf(apj.x, r.y, apj.y * r.x));
+        P[k + j * N] = nk;
+        rowbuf[j] = nk;
+      }
+      __syncthreads();
+      for (int e = tid; e < N * pb; e += T) {
+        const int i = e % N, j = e / N;
+        if (i != k) {
+          float2 v = (j == t) ? make_float2(0.f, 0.f) : P[e];
+          const float2 f = Cm[i + t * N];
+          const float2 rk = rowbuf[j];
+          v.x = fmaf(-f.x, rk.x, v.x);
+          v.x = fmaf(f.y, rk.y, v.x);
+          v.y = fmaf(-f.x, rk.y, v.y);
+          v.y = fmaf(-f.y, rk.x, v.y);
+          P[e] = v;
+        }
+      }
+      __syncthreads();
+    }
+    if (misc[1]) break;
+    for (int j = warp; j < N; j += nwarp) {
+      if (j >= k0 && j < k0 + pb) continue;
+      float2* col = Wf + (size_t)j * N;
+      float2 x[MX_ROWS];
+#pragma unroll
+      for (int q = 0; q < MX_ROWS; ++q) {
+        const int i = lane + 32 * q;
+        x[q] = i < N ? col[i] : make_float2(0.f, 0.f);
+      }
+      for (int t = 0; t < pb; ++t) {
+        const int k = k0 + t, p = perm[k];
+        const float2 r = recip[t];
+        const float2 akj = shfl_f2(pick_f(x, k >> 5), k & 31);
+        const float2 apj = shfl_f2(pick_f(x, p >> 5), p & 31);
+        const float2 nk = make_float2(fmaf(apj.x, r.x, -apj.y * r.y), fmaf(apj.x, r.y, apj.y * r.x));
+        const float2* cm = Cm + t * N;
+#pragma unroll
+        for (int q = 0; q < MX_ROWS; ++q) {
+          const int i = lane + 32 * q;
+          if (i < N && i != k) {
+            float2 v = (i == p) ? akj : x[q];
+            const float2 f = cm[i];
+            v.x = fmaf(-f.x, nk.x, v.x);
+            v.x = fmaf(f.y, nk.y, v.x);
+            v.y = fmaf(-f.x, nk.y, v.y);
+            v.y = fmaf(-f.y, nk.x, v.y);
+            x[q] = v;
+          } else if (i == k) {
+            x[q] = nk;
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < MX_ROWS; ++q) {
+        const int i = lane + 32 * q;
+        if (i < N) col[i] = x[q];
+      }
+    }
+    for (int e = tid; e < N * pb; e += T) Wf[(size_t)k0 * N + e] = P[e];
+    __syncthreads();
+  }
+  const int singular = misc[1];
+  if (tid == 0) {
+    for (int j = 0; j < N; ++j) cols[j] = j;
+    if (!singular) {
+      for (int k = N - 1; k >= 0; --k) {
+        const int p = perm[k];
+        const int t = cols[k];
+        cols[k] = cols[p];
+        cols[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int j = warp; j < N; j += nwarp) {
+    const int cj = cols[j];
+    for (int i = lane; i < N; i += 32) {
+      const size_t e = (size_t)i + (size_t)j * N;
+      if (singular) {
+        G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+      } else {
+        const float2 v = Wf[i + (size_t)cj * N];
+        G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
+      }
+    }
+  }
+  __syncthreads();
+  return singular;
+}
+
 // (w I - X)^-1 into *Gp: FP32 Gauss-Jordan, then Newton-Schulz steps
 // G <- G + G (I - M G) on the split tensor-core products until the residual
 // sum_ij |I - M G|_1 stops shrinking quadratically, or is at most 1e-7 N
 // before an update (after which the residual is ~(1e-7)^2, below the products'
 // own rounding); at most ns_max steps.  Uses Mi, R, Gn as work; swaps *Gp and *Gn.
-__device__ int mixed_inverse(const double2* X, double2 w, int N, int NP, int ns_max, double2** Gp,
-                             double2** Gnp, double2* Mi, double2* R, MxShared& s, MxState& st) {
-  const int sing = gj32_start(X, w, N, Mi, *Gp, s);
+__device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int ns_max,
+                             double2** Gp, double2** Gnp, double2* Mi, double2* R, MxShared& s,
+                             MxState& st) {
+  const int N = pl.N;
+  const int sing = N <= MX_SMEM_GJ_N ? gj32_start(X, w, N, Mi, *Gp, s)
+                                     : gj32_global(X, w, N, Mi, *Gp, reinterpret_cast<float2*>(R), s);
   float prev = 3.0e38f;
   for (int t = 0; t < ns_max && !st.abort; ++t) {
-    const float part = oz_gemm<OZ_IMINUS>(Mi, *Gp, N, NP, R, nullptr, nullptr, s, st);  // R = I - M G
+    const float part = oz_gemm<OZ_IMINUS>(Mi, *Gp, pl, R, nullptr, nullptr, s, st);  // R = I - M G
     const float res = block_sum_f(part, s);
     if (!(res < 0.25f * prev)) break;                 // no longer converging (or NaN)
-    oz_gemm<OZ_ADDTO>(*Gp, R, N, NP, *Gnp, nullptr, *Gp, s, st);                         // Gn = G + G R
+    oz_gemm<OZ_ADDTO>(*Gp, R, pl, *Gnp, nullptr, *Gp, s, st);                         // Gn = G + G R
     double2* tmp = *Gp;
     *Gp = *Gnp;
     *Gnp = tmp;
@@ -712,8 +943,8 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
                                                             int ns_final) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
-  const int NP = (N + 15) & ~15;
-  MxShared s = mx_layout(smraw, NP);
+  const MxPlan pl = mx_plan(N);
+  MxShared s = mx_layout(smraw, N, pl.w0);
   mx_fill_luts(s);
 
   if (tid == 0) {
@@ -774,13 +1005,13 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
     bool conv = false;
     for (int itc = 1; itc <= a.itermax && !st.abort; ++itc) {
       it = itc;
-      if (mixed_inverse(E, w, N, NP, ns_iter, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
-      oz_gemm<OZ_STORE>(Al, G, N, NP, M1, nullptr, nullptr, s, st);
-      oz_gemm<OZ_STORE>(Be, G, N, NP, M2, nullptr, nullptr, s, st);
-      oz_gemm<OZ_ADD2>(M1, Be, N, NP, E, ES, nullptr, s, st);
-      oz_gemm<OZ_ADD2>(M2, Al, N, NP, E, ET, nullptr, s, st);
-      const float part = oz_gemm<OZ_STORE_NORM>(M1, Al, N, NP, Gn, nullptr, nullptr, s, st);
-      oz_gemm<OZ_STORE>(M2, Be, N, NP, R, nullptr, nullptr, s, st);
+      if (mixed_inverse(E, w, pl, ns_iter, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+      oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);
+      oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st);
+      oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);
+      oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st);
+      const float part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st);
+      oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st);
       double2* t0 = Al;
       Al = Gn;
       Gn = t0;
@@ -796,7 +1027,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
     if (!conv) stat |= PT_NOT_CONVERGED;
     const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
     double dl = 0.0, dr = 0.0, db = 0.0;
-    if (mixed_inverse(ES, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    if (mixed_inverse(ES, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
     if (a.gll)
       for (int e = tid; e < NN; e += T) a.gll[(size_t)inst * NN + e] = G[e];
     double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -811,7 +1042,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
                   a.divide_by_pi, spin[0], spin[1], spin[2]);
     }
     __syncthreads();
-    if (mixed_inverse(ET, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    if (mixed_inverse(ET, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
     if (a.grr)
       for (int e = tid; e < NN; e += T) a.grr[(size_t)inst * NN + e] = G[e];
     if (tid == 0) {
@@ -829,7 +1060,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, i
       }
     }
     __syncthreads();
-    if (mixed_inverse(E, w, N, NP, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    if (mixed_inverse(E, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
     if (a.gb)
       for (int e = tid; e < NN; e += T) a.gb[(size_t)inst * NN + e] = G[e];
     if (tid == 0) {
@@ -864,9 +1095,9 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
                                                         const double2* Y, double2* C, double2* ws,
                                                         int ns, int* status) {
   extern __shared__ __align__(1024) unsigned char smraw[];
-  const int NP = (N + 15) & ~15;
+  const MxPlan pl = mx_plan(N);
   const int NN = N * N;
-  MxShared s = mx_layout(smraw, NP);
+  MxShared s = mx_layout(smraw, N, pl.w0);
   mx_fill_luts(s);
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -890,7 +1121,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
   st.abort = 0;
   int sing = 0;
   if (op == 0) {
-    oz_gemm<OZ_STORE>(X, Y, N, NP, C, nullptr, nullptr, s, st);
+    oz_gemm<OZ_STORE>(X, Y, pl, C, nullptr, nullptr, s, st);
   } else {
     // C = X^-1: X given directly, so pass -X with w = 0 (M = 0*I - (-X) = X)
     double2* negX = ws + 4 * (size_t)NN;
@@ -898,7 +1129,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
     __syncthreads();
     double2* G = ws;
     double2* Gn = ws + NN;
-    sing = mixed_inverse(negX, make_double2(0.0, 0.0), N, NP, ns, &G, &Gn, ws + 2 * (size_t)NN,
+    sing = mixed_inverse(negX, make_double2(0.0, 0.0), pl, ns, &G, &Gn, ws + 2 * (size_t)NN,
                          ws + 3 * (size_t)NN, s, st);
     for (int e = tid; e < NN; e += blockDim.x) C[e] = G[e];
   }
@@ -913,16 +1144,20 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
 }
 
 size_t mixed_smem(int N) {
-  const int NP = (N + 15) & ~15;
-  const size_t bufbytes = 2 * NSL * APLANE + 2 * NSL * (size_t)NP * KCH * 2;
-  // the FP32 Gauss-Jordan matrix (N*N float2) aliases the buffers
-  const size_t planes = 2 * bufbytes > (size_t)(N + 1) * N * 8 ? 2 * bufbytes : (size_t)(N + 1) * N * 8;
-  return planes + 128 * 8 * 2 + 16 + 128 * 4 * 4 + 32 * 4 + 16 + 8 + 16 + 2 * NSL * 128 * 2;
+  const MxPlan pl = mx_plan(N);
+  const size_t bufbytes = (size_t)bufbytes_of(pl.w0);
+  // the FP32 Gauss-Jordan matrix ((N+1)*N float2, Ndim <= MX_SMEM_GJ_N) or the
+  // panel and multiplier columns (2 * N * MX_PANEL float2) alias the buffers
+  size_t planes = 2 * bufbytes;
+  const size_t gj = N <= MX_SMEM_GJ_N ? (size_t)(N + 1) * N * 8 : (size_t)2 * N * MX_PANEL * 8;
+  if (gj > planes) planes = gj;
+  return planes + (size_t)MX_MAXN * 8 * 2 + MX_PANEL * 8 + (size_t)MX_MAXN * 4 * 4 + 32 * 4 +
+         16 + 8 + 16 + 2 * NSL * 128 * 2;
 }
 
 }  // namespace
 
-int decim_mixed_max_n() { return 112; }     // double-buffered 7-digit planes fill shared memory
+int decim_mixed_max_n() { return MX_MAXN; }
 
 size_t decim_mixed_ws_matrices() { return 11; }
 
