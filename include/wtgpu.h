@@ -62,7 +62,7 @@ extern "C" {
 #define WTG_PREC_MIXED 1        /* products as exact BF16 digit splits on the tcgen05 tensor
                                    cores (49-bit operands, FP32 accumulation exact per slice
                                    order, int64 recombination), inverses FP32 Gauss-Jordan +
-                                   Newton-Schulz refinement on those products; Ndim <= 112 */
+                                   Newton-Schulz refinement on those products; Ndim <= 320 */
 
 typedef struct wtg_model* wtg_model_t;
 
@@ -236,6 +236,57 @@ int wtg_last_error(char* buf, int len);
 
 /* Describe the device the library runs on ("name, SMs, cc") into buf. */
 int wtg_device_info(char* buf, int len);
+
+/*
+ * Uneven batches: (k, omega, eta) points of several resident models, of
+ * different Ndim, solved in ONE persistent kernel launch.  The CTAs take the
+ * points in order of estimated cost (Ndim^3 x an iteration estimate growing as
+ * eta shrinks, largest first); each point runs its own Fourier sum (as
+ * wtg_ham_qlayer2qlayer) and decimation (as wtg_surface_spectrum) and stops at
+ * its own convergence, so one result never depends on the other points of the
+ * batch.  No counterpart in the reference, which solves one (k, omega) at a
+ * time (src/surfstat.f90:123-160, src/fermiarc.f90:206-248); the per-point
+ * arithmetic is the same as wtg_surface_spectrum's.
+ *
+ * An engine holds the device tables of a fixed model set, a workspace sized for
+ * the largest Ndim, pinned staging and its own stream; it runs one batch at a
+ * time and several engines run concurrently (a serving loop keeps one per
+ * in-flight batch).
+ *   models[nmodels]      handles of one device (they must outlive the engine)
+ *   precision            WTG_PREC_FP64 or WTG_PREC_MIXED
+ *   max_points           largest npts of one run
+ *   ntop[nmodels], top   per-model TopOrbitals lists, concatenated (1-based)
+ *   nbot[nmodels], bot   per-model BottomOrbitals lists, concatenated
+ */
+typedef struct wtg_engine* wtg_engine_t;
+
+int wtg_engine_create(int nmodels, const wtg_model_t* models, int precision, int max_points,
+                      const int* ntop, const int* top, const int* nbot, const int* bot,
+                      wtg_engine_t* engine);
+int wtg_engine_destroy(wtg_engine_t engine);
+/* Device bytes the engine holds, its max_points and the kernels it launched (any may be NULL). */
+int wtg_engine_info(wtg_engine_t engine, long long* device_bytes, int* max_points,
+                    long long* launches);
+/*
+ * One batch (host buffers, synchronous):
+ *   point_model[npts]          index into the engine's models
+ *   k[npts*2]                  column-major (npts, 2) fractional in-plane k
+ *   omega[npts], eta[npts]     Hartree
+ *   tol, itermax, divide_by_pi as wtg_surface_spectrum
+ *   dos_l/dos_r/dos_bulk[npts] out; iters[npts], status[npts] out (may be NULL)
+ * Returns the number of flagged points (>= 0) or a negative error code.
+ */
+int wtg_engine_run(wtg_engine_t engine, int npts, const int* point_model, const double* k,
+                   const double* omega, const double* eta, double tol, int itermax,
+                   int divide_by_pi, double* dos_l, double* dos_r, double* dos_bulk, int* iters,
+                   unsigned char* status);
+
+/* One-shot: create an engine for these models and points, run, destroy. */
+int wtg_batch_spectrum(int nmodels, const wtg_model_t* models, int npts, const int* point_model,
+                       const double* k, const double* omega, const double* eta, double tol,
+                       int itermax, const int* ntop, const int* top, const int* nbot,
+                       const int* bot, int divide_by_pi, int precision, double* dos_l,
+                       double* dos_r, double* dos_bulk, int* iters, unsigned char* status);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,15 @@ SIGNATURES = {
     "wtg_surfgreen_batch_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_double,
                                                C.c_double, C.c_int, C.c_int, _ip, C.c_int, _ip, C.c_int,
                                                _vp, _vp, _vp, _vp, _vp, _vp]),
+    "wtg_engine_create": (C.c_int, [C.c_int, C.POINTER(_vp), C.c_int, C.c_int, _ip, _ip, _ip, _ip,
+                                     C.POINTER(_vp)]),
+    "wtg_engine_destroy": (C.c_int, [_vp]),
+    "wtg_engine_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), _ip, C.POINTER(C.c_longlong)]),
+    "wtg_engine_run": (C.c_int, [_vp, C.c_int, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                  _dp, _dp, _dp, _i32p, _u8p]),
+    "wtg_batch_spectrum": (C.c_int, [C.c_int, C.POINTER(_vp), C.c_int, _ip, _dp, _dp, _dp, C.c_double,
+                                      C.c_int, _ip, _ip, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp,
+                                      _i32p, _u8p]),
     "wtg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "wtg_device_info": (C.c_int, [C.c_char_p, C.c_int]),
 }

@@ -216,6 +216,108 @@ class Model:
         return {"fourier_ms": f.value, "decim_ms": d.value, "launches": int(n.value),
                 "decim_launches": int(nd.value)}
 
+def _lists(models, tops, bots):
+    ntop = np.ascontiguousarray([len(t) for t in tops], dtype=np.int32)
+    nbot = np.ascontiguousarray([len(b) for b in bots], dtype=np.int32)
+    top = np.ascontiguousarray(np.concatenate([np.asarray(t, np.int32) for t in tops] + [np.zeros(1, np.int32)]))
+    bot = np.ascontiguousarray(np.concatenate([np.asarray(b, np.int32) for b in bots] + [np.zeros(1, np.int32)]))
+    if len(tops) != len(models) or len(bots) != len(models):
+        raise ValueError("one top and one bottom orbital list per model")
+    return ntop, top, nbot, bot
+
+
+def _points(point_model, kpts, omega, eta):
+    pm = np.ascontiguousarray(point_model, dtype=np.int32).ravel()
+    n = len(pm)
+    kk = np.asarray(kpts, dtype=np.float64).reshape(n, 2)
+    kcol = np.ascontiguousarray(kk.T).ravel()                  # (npts, 2) column-major
+    om = np.ascontiguousarray(np.broadcast_to(np.asarray(omega, np.float64), (n,)))
+    et = np.ascontiguousarray(np.broadcast_to(np.asarray(eta, np.float64), (n,)))
+    return pm, kcol, om, et
+
+
+class Engine:
+    """A batch engine (wtg_engine_create): device tables of a fixed model set, a
+    workspace for their largest Ndim and its own stream.  ``run`` solves points
+    of several models (uneven Ndim, eta per point) in one persistent launch.
+    One engine runs one batch at a time; separate engines run concurrently."""
+
+    def __init__(self, models, tops, bots, precision: int = PREC_FP64, max_points: int = 4096):
+        lib = _lib.load()
+        self.models = list(models)
+        self._ntop, self._top, self._nbot, self._bot = _lists(self.models, tops, bots)
+        arr = (C.c_void_p * len(self.models))(*[m._handle.value for m in self.models])
+        self._arr = arr
+        h = C.c_void_p()
+        check(lib.wtg_engine_create(len(self.models), arr, int(precision), int(max_points),
+                                    _iptr(self._ntop), _iptr(self._top), _iptr(self._nbot),
+                                    _iptr(self._bot), C.byref(h)))
+        self._handle = h
+        self.precision = int(precision)
+        self.max_points = int(max_points)
+
+    def info(self) -> dict:
+        b = C.c_longlong(0)
+        mp = C.c_int(0)
+        la = C.c_longlong(0)
+        check(_lib.load().wtg_engine_info(self._handle, C.byref(b), C.byref(mp), C.byref(la)))
+        return {"device_bytes": int(b.value), "max_points": int(mp.value), "launches": int(la.value)}
+
+    def run(self, point_model, kpts, omega, eta, tol: float = ACCURACY_REF,
+            itermax: int = ITERMAX_REF, divide_by_pi: bool = False) -> dict:
+        """Per point: dos_l, dos_r, dos_bulk, iters, status (arrays of npts)."""
+        pm, kcol, om, et = _points(point_model, kpts, omega, eta)
+        n = len(pm)
+        out = {name: np.empty(n, np.float64) for name in ("dos_l", "dos_r", "dos_bulk")}
+        out["iters"] = np.empty(n, np.int32)
+        out["status"] = np.empty(n, np.uint8)
+        check(_lib.load().wtg_engine_run(
+            self._handle, n, _iptr(pm), _dptr(kcol), _dptr(om), _dptr(et), float(tol), int(itermax),
+            1 if divide_by_pi else 0, _dptr(out["dos_l"]), _dptr(out["dos_r"]), _dptr(out["dos_bulk"]),
+            out["iters"].ctypes.data_as(C.POINTER(C.c_int32)),
+            out["status"].ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out
+
+    def close(self):
+        if getattr(self, "_handle", None) is not None and self._handle.value:
+            _lib.load().wtg_engine_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def batch_spectrum(models, tops, bots, point_model, kpts, omega, eta, tol: float = ACCURACY_REF,
+                   itermax: int = ITERMAX_REF, divide_by_pi: bool = False,
+                   precision: int = PREC_FP64) -> dict:
+    """One uneven batch (wtg_batch_spectrum): point p of model point_model[p]
+    at kpts[p], omega[p], eta[p] (Hartree); per-point outputs."""
+    models = list(models)
+    ntop, top, nbot, bot = _lists(models, tops, bots)
+    pm, kcol, om, et = _points(point_model, kpts, omega, eta)
+    n = len(pm)
+    out = {name: np.empty(n, np.float64) for name in ("dos_l", "dos_r", "dos_bulk")}
+    out["iters"] = np.empty(n, np.int32)
+    out["status"] = np.empty(n, np.uint8)
+    arr = (C.c_void_p * len(models))(*[m._handle.value for m in models])
+    check(_lib.load().wtg_batch_spectrum(
+        len(models), arr, n, _iptr(pm), _dptr(kcol), _dptr(om), _dptr(et), float(tol), int(itermax),
+        _iptr(ntop), _iptr(top), _iptr(nbot), _iptr(bot), 1 if divide_by_pi else 0, int(precision),
+        _dptr(out["dos_l"]), _dptr(out["dos_r"]), _dptr(out["dos_bulk"]),
+        out["iters"].ctypes.data_as(C.POINTER(C.c_int32)),
+        out["status"].ctypes.data_as(C.POINTER(C.c_uint8))))
+    return out
+
+
 def surfgreen_1985(omega: float, h00: np.ndarray, h01: np.ndarray, eta: float,
                    tol: float = ACCURACY_REF, itermax: int = ITERMAX_REF):
     """One decimation on the GPU: (GLL, GRR, GB, iters, status)."""

@@ -7,6 +7,7 @@
 // in wtg_fourier.cu / wtg_decimate.cu.
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -227,6 +228,252 @@ int count_flagged(const uint8_t* st, size_t n) {
   long long c = 0;
   for (size_t i = 0; i < n; ++i) c += st[i] != 0;
   return (int)std::min<long long>(c, INT_MAX);
+}
+
+}  // namespace
+
+// A batch engine: the device tables of a fixed set of models, one workspace
+// sized for their largest Ndim, its own stream and staging.  One engine runs
+// one batch at a time (calls are serialised by its mutex); several engines
+// run concurrently on one device.
+struct wtg_engine {
+  int device = 0;
+  int precision = 0;
+  int nmodels = 0;
+  int max_points = 0;
+  int max_n = 0;
+  std::vector<int> model_n;
+  wtg::DecimConfig cfg;
+  int smem_gj_max = 0, wb = 0;
+  size_t ph_off = 0;
+  int grid = 0;
+  size_t ws_stride = 0;
+  DevBuf models_d, lists_d, ws, io_d, counter;
+  unsigned char* pinned = nullptr;
+  size_t in_bytes = 0, out_bytes = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  long long launches = 0;
+  size_t device_bytes = 0;
+  ~wtg_engine() {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    models_d.release();
+    lists_d.release();
+    ws.release();
+    io_d.release();
+    counter.release();
+    if (pinned) cudaFreeHost(pinned);
+    if (stream) cudaStreamDestroy(stream);
+    cudaSetDevice(cur);
+  }
+};
+
+namespace {
+
+// per-point input block (device and pinned host): pmodel, order, k (npts x 2), omega, eta;
+// output block: dos_l, dos_r, dos_bulk, iters, status
+size_t engine_in_bytes(int n) { return (size_t)n * (4 + 4 + 16 + 8 + 8); }
+size_t engine_out_bytes(int n) { return (size_t)n * (8 * 3 + 4 + 1); }
+
+int engine_create(int nmodels, const wtg_model_t* models, int precision, int max_points,
+                  const int* ntop, const int* top, const int* nbot, const int* bot,
+                  wtg_engine_t* out) {
+  if (!out) return fail(WTG_EINVAL, "out is null");
+  *out = nullptr;
+  if (nmodels < 1 || !models || max_points < 1 || !ntop || !nbot)
+    return fail(WTG_EINVAL, "bad argument");
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
+  const bool mixed = precision == WTG_PREC_MIXED;
+  int max_n = 0, max_nru = 1, dev = -1;
+  for (int i = 0; i < nmodels; ++i) {
+    if (!models[i]) return fail(WTG_EINVAL, "null model");
+    if (dev >= 0 && models[i]->device != dev) return fail(WTG_EINVAL, "models on different devices");
+    dev = models[i]->device;
+    max_n = std::max(max_n, models[i]->N);
+    max_nru = std::max(max_nru, models[i]->nRu);
+  }
+  const int nmax = mixed ? wtg::decim_mixed_max_n() : wtg::decim_fp64_large_max_n();
+  if (max_n > nmax)
+    return fail(WTG_EUNSUPPORTED, "Ndim " + std::to_string(max_n) + " exceeds the kernel limit " +
+                                      std::to_string(nmax));
+  // orbital lists: check each model's slice
+  {
+    size_t ot = 0, ob = 0;
+    for (int i = 0; i < nmodels; ++i) {
+      const int rc = check_lists(models[i]->nw, ntop[i], top ? top + ot : nullptr, nbot[i],
+                                 bot ? bot + ob : nullptr);
+      if (rc != WTG_OK) return rc;
+      ot += (size_t)ntop[i];
+      ob += (size_t)nbot[i];
+    }
+  }
+  WTG_CK(cudaSetDevice(dev));
+  auto* e = new wtg_engine();
+  e->device = dev;
+  e->precision = precision;
+  e->nmodels = nmodels;
+  e->max_points = max_points;
+  e->max_n = max_n;
+  const size_t ph_bytes = (size_t)max_nru * sizeof(double2);
+  cudaError_t ce;
+  if (mixed) {
+    ce = wtg::batch_mixed_config(max_n, &e->wb, &e->cfg);
+  } else {
+    ce = wtg::batch_fp64_config(max_n, ph_bytes, &e->smem_gj_max, &e->cfg);
+  }
+  if (ce != cudaSuccess) {
+    delete e;
+    return cuda_fail(ce, "batch config");
+  }
+  e->ph_off = (e->cfg.smem + 15) & ~(size_t)15;
+  e->cfg.smem = e->ph_off + ph_bytes;
+  int optin = 0, nsm = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e->cfg.smem > (size_t)optin) {
+    delete e;
+    return fail(WTG_EUNSUPPORTED, "batch kernel shared memory exceeds the device limit");
+  }
+  e->grid = nsm * std::max(1, e->cfg.ctas_per_sm);
+  e->ws_stride = wtg::batch_ws_matrices(mixed ? 1 : 0) * (size_t)max_n * max_n;
+  // device tables
+  std::vector<int> lists;
+  size_t ot = 0, ob = 0;
+  std::vector<size_t> toff(nmodels), boff(nmodels);
+  for (int i = 0; i < nmodels; ++i) {
+    toff[i] = lists.size();
+    for (int q = 0; q < ntop[i]; ++q) lists.push_back(top[ot + q]);
+    ot += (size_t)ntop[i];
+    boff[i] = lists.size();
+    for (int q = 0; q < nbot[i]; ++q) lists.push_back(bot[ob + q]);
+    ob += (size_t)nbot[i];
+  }
+  if (lists.empty()) lists.push_back(0);
+  ce = e->lists_d.ensure(sizeof(int) * lists.size());
+  if (ce == cudaSuccess)
+    ce = cudaMemcpy(e->lists_d.p, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice);
+  std::vector<wtg::BatchModel> bm(nmodels);
+  for (int i = 0; i < nmodels && ce == cudaSuccess; ++i) {
+    const wtg_model* m = models[i];
+    wtg::BatchModel& b = bm[i];
+    b.N = m->N;
+    b.nw = m->nw;
+    b.np = m->np;
+    b.nRu = m->nRu;
+    b.nic = m->nic;
+    b.ic_lo = m->ic_lo;
+    b.hr = m->d_hr;
+    b.rab = m->d_rab;
+    b.icoff = m->d_icoff;
+    b.ntop = ntop[i];
+    b.nbot = nbot[i];
+    b.top = (const int*)e->lists_d.p + toff[i];
+    b.bot = (const int*)e->lists_d.p + boff[i];
+    e->model_n.push_back(m->N);
+  }
+  if (ce == cudaSuccess) ce = e->models_d.ensure(sizeof(wtg::BatchModel) * nmodels);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpy(e->models_d.p, bm.data(), sizeof(wtg::BatchModel) * nmodels, cudaMemcpyHostToDevice);
+  e->in_bytes = engine_in_bytes(max_points);
+  e->out_bytes = engine_out_bytes(max_points);
+  const size_t ws_bytes = sizeof(double2) * e->ws_stride * e->grid;
+  if (ce == cudaSuccess) ce = e->ws.ensure(ws_bytes);
+  if (ce == cudaSuccess) ce = e->io_d.ensure(e->in_bytes + e->out_bytes);
+  if (ce == cudaSuccess) ce = e->counter.ensure(64);
+  if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->pinned, e->in_bytes + e->out_bytes);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    delete e;
+    return cuda_fail(ce, "wtg_engine_create");
+  }
+  e->device_bytes = ws_bytes + e->in_bytes + e->out_bytes + sizeof(int) * lists.size() +
+                    sizeof(wtg::BatchModel) * nmodels + 64;
+  *out = e;
+  return WTG_OK;
+}
+
+int engine_run(wtg_engine* e, int npts, const int* point_model, const double* k,
+               const double* omega, const double* eta, double tol, int itermax, int divide_by_pi,
+               double* dos_l, double* dos_r, double* dos_bulk, int* iters, unsigned char* status) {
+  if (!e) return fail(WTG_EINVAL, "null engine");
+  if (npts < 0 || npts > e->max_points) return fail(WTG_EINVAL, "npts outside 0..max_points");
+  if (itermax < 0) return fail(WTG_EINVAL, "itermax < 0");
+  if (npts == 0) return WTG_OK;
+  if (!point_model || !k || !omega || !eta || !dos_l || !dos_r || !dos_bulk)
+    return fail(WTG_EINVAL, "null array");
+  for (int p = 0; p < npts; ++p)
+    if (point_model[p] < 0 || point_model[p] >= e->nmodels)
+      return fail(WTG_EINVAL, "point_model outside 0..nmodels-1");
+  std::lock_guard<std::mutex> lk(e->mu);
+  WTG_CK(cudaSetDevice(e->device));
+  // launch order: largest estimated cost first (Ndim^3 x an iteration estimate that
+  // grows as eta shrinks), so the persistent CTAs finish together
+  std::vector<int> order(npts);
+  std::vector<double> cost(npts);
+  for (int p = 0; p < npts; ++p) {
+    const double n = (double)e->model_n[point_model[p]];
+    const double ev = std::max(1e-12, std::fabs(eta[p]) * 27.211385);
+    cost[p] = n * n * n * (1.0 + std::max(0.0, -std::log10(ev)));
+    order[p] = p;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  // stage inputs: pmodel | order | k (npts x 2) | omega | eta, for npts points
+  unsigned char* h = e->pinned;
+  const size_t n = (size_t)npts;
+  memcpy(h, point_model, 4 * n);
+  memcpy(h + 4 * n, order.data(), 4 * n);
+  memcpy(h + 8 * n, k, 16 * n);
+  memcpy(h + 24 * n, omega, 8 * n);
+  memcpy(h + 32 * n, eta, 8 * n);
+  unsigned char* d = (unsigned char*)e->io_d.p;
+  cudaStream_t s = e->stream;
+  WTG_CK(cudaMemcpyAsync(d, h, 40 * n, cudaMemcpyHostToDevice, s));
+  unsigned char* dout = d + e->in_bytes;
+  WTG_CK(cudaMemsetAsync(e->counter.p, 0, sizeof(int), s));
+  wtg::BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.npts = npts;
+  a.models = (const wtg::BatchModel*)e->models_d.p;
+  a.pmodel = (const int*)d;
+  a.order = (const int*)(d + 4 * n);
+  a.k = (const double*)(d + 8 * n);
+  a.omega = (const double*)(d + 24 * n);
+  a.eta = (const double*)(d + 32 * n);
+  a.tol = tol;
+  a.itermax = itermax;
+  a.divide_by_pi = divide_by_pi ? 1 : 0;
+  a.dos_l = (double*)dout;
+  a.dos_r = (double*)(dout + 8 * n);
+  a.dos_bulk = (double*)(dout + 16 * n);
+  a.iters = (int32_t*)(dout + 24 * n);
+  a.status = (uint8_t*)(dout + 28 * n);
+  a.ws = (double2*)e->ws.p;
+  a.ws_stride = e->ws_stride;
+  a.counter = (int*)e->counter.p;
+  a.KC = e->cfg.KC;
+  a.smem_gj_max = e->smem_gj_max;
+  a.wb = e->wb;
+  a.ph_off = e->ph_off;
+  const int grid = std::min(e->grid, npts);
+  if (e->precision == WTG_PREC_MIXED) {
+    WTG_CK(wtg::launch_batch_mixed(a, e->cfg, grid, s));
+  } else {
+    WTG_CK(wtg::launch_batch_fp64(a, e->cfg, grid, s));
+  }
+  e->launches += 1;
+  unsigned char* hout = h + e->in_bytes;
+  WTG_CK(cudaMemcpyAsync(hout, dout, 29 * n, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  memcpy(dos_l, hout, 8 * n);
+  memcpy(dos_r, hout + 8 * n, 8 * n);
+  memcpy(dos_bulk, hout + 16 * n, 8 * n);
+  if (iters) memcpy(iters, hout + 24 * n, 4 * n);
+  if (status) memcpy(status, hout + 28 * n, n);
+  return count_flagged(hout + 28 * n, n);
 }
 
 }  // namespace
@@ -653,6 +900,49 @@ int wtg_device_info(char* buf, int len) {
   snprintf(buf, (size_t)len, "%s, %d SMs, cc %d.%d, %.1f GiB", p.name, p.multiProcessorCount,
            p.major, p.minor, p.totalGlobalMem / 1073741824.0);
   return WTG_OK;
+}
+
+int wtg_engine_create(int nmodels, const wtg_model_t* models, int precision, int max_points,
+                      const int* ntop, const int* top, const int* nbot, const int* bot,
+                      wtg_engine_t* out) {
+  return engine_create(nmodels, models, precision, max_points, ntop, top, nbot, bot, out);
+}
+
+int wtg_engine_destroy(wtg_engine_t e) {
+  if (!e) return fail(WTG_EINVAL, "null engine");
+  delete e;
+  return WTG_OK;
+}
+
+int wtg_engine_info(wtg_engine_t e, long long* device_bytes, int* max_points, long long* launches) {
+  if (!e) return fail(WTG_EINVAL, "null engine");
+  if (device_bytes) *device_bytes = (long long)e->device_bytes;
+  if (max_points) *max_points = e->max_points;
+  if (launches) *launches = e->launches;
+  return WTG_OK;
+}
+
+int wtg_engine_run(wtg_engine_t e, int npts, const int* point_model, const double* k,
+                   const double* omega, const double* eta, double tol, int itermax,
+                   int divide_by_pi, double* dos_l, double* dos_r, double* dos_bulk, int* iters,
+                   unsigned char* status) {
+  return engine_run(e, npts, point_model, k, omega, eta, tol, itermax, divide_by_pi, dos_l, dos_r,
+                    dos_bulk, iters, status);
+}
+
+int wtg_batch_spectrum(int nmodels, const wtg_model_t* models, int npts, const int* point_model,
+                       const double* k, const double* omega, const double* eta, double tol,
+                       int itermax, const int* ntop, const int* top, const int* nbot,
+                       const int* bot, int divide_by_pi, int precision, double* dos_l,
+                       double* dos_r, double* dos_bulk, int* iters, unsigned char* status) {
+  if (npts == 0) return WTG_OK;
+  wtg_engine_t e = nullptr;
+  int rc = engine_create(nmodels, models, precision, std::max(1, npts), ntop, top, nbot, bot, &e);
+  if (rc != WTG_OK) return rc;
+  rc = engine_run(e, npts, point_model, k, omega, eta, tol, itermax, divide_by_pi, dos_l, dos_r,
+                  dos_bulk, iters, status);
+  delete e;
+  return rc;
 }
 
 }  // extern "C"

@@ -118,6 +118,43 @@ struct DecimArgs {
   int bot[MAX_ORB];
 };
 
+// Uneven batch (several models, one launch): per-model tables, device-resident
+struct BatchModel {
+  int N, nw, np;
+  int nRu, nic, ic_lo;        // Fourier tables as FourierArgs
+  const double2* hr;
+  const double2* rab;
+  const int* icoff;
+  int ntop, nbot;
+  const int* top;             // 1-based orbital lists, device
+  const int* bot;
+};
+
+struct BatchArgs {
+  int npts;
+  const BatchModel* models;   // device
+  const int* pmodel;          // [npts] model of each point
+  const int* order;           // [npts] points in launch order (largest estimated cost first)
+  const double* k;            // (npts, 2) column-major
+  const double* omega;        // [npts]
+  const double* eta;          // [npts]
+  double tol;
+  int itermax;
+  int divide_by_pi;
+  double* dos_l;              // [npts]
+  double* dos_r;
+  double* dos_bulk;
+  int32_t* iters;             // may be null
+  uint8_t* status;            // may be null
+  double2* ws;                // [grid][ws_stride]
+  size_t ws_stride;           // double2 per CTA
+  int* counter;               // zero at launch
+  int KC;                     // FP64 GEMM k-chunk
+  int smem_gj_max;            // FP64: largest Ndim whose inverse runs in shared memory
+  int wb;                     // mixed: B-plane width of the shared-memory layout
+  size_t ph_off;              // byte offset of the phase table (max nRu double2) in shared memory
+};
+
 struct DecimConfig {
   int threads;
   int KC;
@@ -149,6 +186,16 @@ size_t decim_mixed_ws_matrices();
 cudaError_t decim_mixed_config(int N, DecimConfig* cfg);
 cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                   cudaStream_t s);
+
+// Uneven batch launch shapes and launches.  The configs' shared memory excludes the
+// phase table, which the caller appends at BatchArgs::ph_off and adds to cfg.smem before
+// launching; extra_smem reserves room for it.
+cudaError_t batch_fp64_config(int max_n, size_t extra_smem, int* smem_gj_max, DecimConfig* cfg);
+cudaError_t launch_batch_fp64(const BatchArgs& a, const DecimConfig& cfg, int grid, cudaStream_t s);
+cudaError_t batch_mixed_config(int max_n, int* wb, DecimConfig* cfg);
+cudaError_t launch_batch_mixed(const BatchArgs& a, const DecimConfig& cfg, int grid, cudaStream_t s);
+// Workspace matrices per CTA of the batch kernels.
+size_t batch_ws_matrices(int precision_mixed);
 
 // One product (op 0: C = X*Y) or inverse (op 1: C = X^-1) by a single CTA.
 // Mixed: ws holds 5 N x N complex matrices; FP64: work holds two.

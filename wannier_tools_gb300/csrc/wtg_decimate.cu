@@ -21,6 +21,8 @@
 // memory in k-chunks, and the inverse runs in shared memory.  What matters is
 // the count of FP64 instructions (exactly 4 DFMA per complex multiply-add)
 // and keeping the pipe fed; pivot searches compare magnitudes as integers.
+#include <algorithm>
+
 #include "wtg_common.cuh"
 
 namespace wtg {
@@ -29,21 +31,134 @@ namespace {
 
 #include "wtg_fp64_dev.cuh"
 
+// Options of one solve for the batch kernel, with the member names of
+// DecimArgs (whose kernel parameter the plain kernel passes directly, so its
+// lists are read from parameter space).  Orbital lists are 1-based.
+struct SolveOpts {
+  int nw;
+  double tol;
+  int itermax;
+  int divide_by_pi;
+  int ntop, nbot;
+  const int* top;
+  const int* bot;
+  double* spin[6];             // null: no spin-resolved sums
+  int spin_right_bottom;
+};
+
+// Decimation of one instance whose eps, eps_s, eps_t (= H00), alpha (= H01)
+// and beta (= H01^dagger) already sit in workspace matrices 0..4 of W; the
+// spectral sums of the three final inverses are handed to emit(dl, dr, db,
+// spin[6], iterations, status) in thread 0, the inverses themselves go to
+// gll / grr / gb when those are not null.
 // GI = false: the inverse runs in shared memory (Ndim <= decim_fp64_max_n());
-// GI = true: it runs in a ninth workspace matrix in global memory, in panels
+// GI = true: it runs in workspace matrix 8 in global memory, in panels
 // (gj_invert_global; Ndim <= 320).
-template <int RP, bool GI>
-__global__ void __launch_bounds__(GI ? 256 : 512, 1) k_decimate_fp64(const DecimArgs a) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
-  const Shared s = fp64_layout(smraw, N, a.KC, !GI);
-  double2* W = a.ws + (size_t)blockIdx.x * (GI ? 9 : 8) * NN;
+template <int RP, bool GI, class O, class Emit>
+__device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, double2* grr,
+                           double2* gb, double2* W, const Shared& s, Emit emit) {
+  const int NN = N * N, tid = threadIdx.x;
   double2* Mg = GI ? W + (size_t)8 * NN : nullptr;   // global-memory inverse work
   double2* E = W;
   double2* ES = W + (size_t)NN;
   double2* ET = W + (size_t)2 * NN;
-  double2* bufs[5] = {W + (size_t)3 * NN, W + (size_t)4 * NN, W + (size_t)5 * NN,
-                      W + (size_t)6 * NN, W + (size_t)7 * NN};
+  double2* Al = W + (size_t)3 * NN;
+  double2* Be = W + (size_t)4 * NN;
+  double2* G = W + (size_t)5 * NN;
+  double2* M1 = W + (size_t)6 * NN;
+  double2* M2 = W + (size_t)7 * NN;
+  // (w - X)^-1, optionally stored un-permuted to dst; ginv reads the result
+  auto invert = [&](const double2* X, double2* dst) -> int {
+    int sing;
+    if (GI) {
+      sing = gj_invert_global(X, w, N, Mg, s);
+      if (dst) gj_store_global(N, Mg, s, dst);
+    } else {
+      sing = gj_invert(X, w, N, s);
+      if (dst) gj_store(N, s, dst);
+    }
+    return sing;
+  };
+  auto ginv = [&](int i, int j) {
+    return GI ? Mg[i + (size_t)s.cols[j] * N] : s.big[i + s.cols[j] * N];
+  };
+
+  int st = 0, it = 0;
+  bool conv = false;
+  for (int itc = 1; itc <= o.itermax; ++itc) {                // src/surfgreen.f90:86
+    it = itc;
+    if (invert(E, G)) st |= PT_SINGULAR;                      // :88-89
+    __syncthreads();
+    cta_gemm<RP, EPI_STORE>(Al, G, N, KC, s.sX, s.sY, M1, nullptr);     // :92
+    cta_gemm<RP, EPI_STORE>(Be, G, N, KC, s.sX, s.sY, M2, nullptr);     // :95
+    cta_gemm<RP, EPI_ADD2>(M1, Be, N, KC, s.sX, s.sY, E, ES);           // :98-102
+    cta_gemm<RP, EPI_ADD2>(M2, Al, N, KC, s.sX, s.sY, E, ET);           // :107-110
+    double part = cta_gemm<RP, EPI_STORE_NORM>(M1, Al, N, KC, s.sX, s.sY, G, nullptr);  // :113
+    cta_gemm<RP, EPI_STORE>(M2, Be, N, KC, s.sX, s.sY, M1, nullptr);    // :116
+    // rotate buffers: alpha <- G, beta <- M1
+    double2* t0 = Al;
+    Al = G;
+    G = t0;
+    double2* t1 = Be;
+    Be = M1;
+    M1 = t1;
+    const double nrm = block_sum(part, s);                    // :120
+    if (nrm <= o.tol) {                                       // :121
+      conv = true;
+      break;
+    }
+  }
+  if (!conv) st |= PT_NOT_CONVERGED;
+
+  double dl = 0.0, dr = 0.0, db = 0.0;
+  double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  // GLL = (w - eps_s)^-1                                     // :127-128
+  if (invert(ES, gll)) st |= PT_SINGULAR;
+  if (tid == 0) {
+    for (int q = 0; q < o.ntop; ++q) {
+      const int io = o.top[q] - 1;
+      const double v = ginv(io, io).y;
+      dl = o.divide_by_pi ? dl - v / PI_REF : dl - v;
+    }
+    if (o.spin[0])                                            // src/surfstat.f90:162-177
+      spin_sums(ginv, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[0], spin[1], spin[2]);
+  }
+  __syncthreads();
+  // GRR = (w - eps_t)^-1                                     // :130-131
+  if (invert(ET, grr)) st |= PT_SINGULAR;
+  if (tid == 0) {
+    for (int q = 0; q < o.nbot; ++q) {
+      const int io = N - o.nw + o.bot[q] - 1;
+      const double v = ginv(io, io).y;
+      dr = o.divide_by_pi ? dr - v / PI_REF : dr - v;
+    }
+    if (o.spin[0]) {                                          // src/surfstat.f90:178-192
+      if (o.spin_right_bottom)                                // src/fermiarc.f90:300-327
+        spin_sums(ginv, o.nw, o.nbot, o.bot, N - o.nw, o.divide_by_pi, spin[3], spin[4], spin[5]);
+      else
+        spin_sums(ginv, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[3], spin[4], spin[5]);
+    }
+  }
+  __syncthreads();
+  // GB = (w - eps)^-1                                        // :133-134
+  if (invert(E, gb)) st |= PT_SINGULAR;
+  if (tid == 0) {
+    for (int i = 0; i < N; ++i) {
+      const double v = ginv(i, i).y;
+      db = o.divide_by_pi ? db - v / PI_REF : db - v;
+    }
+    if (!isfinite(dl) || !isfinite(dr) || !isfinite(db)) st |= PT_NONFINITE;
+    emit(dl, dr, db, spin, it, st);
+  }
+  __syncthreads();
+}
+
+template <int RP, bool GI>
+__global__ void __launch_bounds__(GI ? 256 : 512, 1) k_decimate_fp64(const __grid_constant__ DecimArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
+  const Shared s = fp64_layout(smraw, N, a.KC, !GI);
+  double2* W = a.ws + (size_t)blockIdx.x * (GI ? 9 : 8) * NN;
 
   for (;;) {
     if (tid == 0) s.misc[0] = atomicAdd(a.counter, 1);
@@ -55,115 +170,77 @@ __global__ void __launch_bounds__(GI ? 256 : 512, 1) k_decimate_fp64(const Decim
     const double2* H00 = a.h + (size_t)ik * 2 * NN;
     const double2* H01 = H00 + NN;
     const double2 w = make_double2(a.omega[iw], a.eta);     // src/surfgreen.f90:82
-    // (w - X)^-1, optionally stored un-permuted to out; ginv reads the result
-    auto invert = [&](const double2* X, double2* out) -> int {
-      int sing;
-      if (GI) {
-        sing = gj_invert_global(X, w, N, Mg, s);
-        if (out) gj_store_global(N, Mg, s, out);
-      } else {
-        sing = gj_invert(X, w, N, s);
-        if (out) gj_store(N, s, out);
-      }
-      return sing;
-    };
-    auto ginv = [&](int i, int j) {
-      return GI ? Mg[i + (size_t)s.cols[j] * N] : s.big[i + s.cols[j] * N];
-    };
-
-    double2* Al = bufs[0];
-    double2* Be = bufs[1];
-    double2* G = bufs[2];
-    double2* M1 = bufs[3];
-    double2* M2 = bufs[4];
     for (int e = tid; e < NN; e += T) {                       // src/surfgreen.f90:74-78
       const double2 h = H00[e];
-      E[e] = h;
-      ES[e] = h;
-      ET[e] = h;
-      Al[e] = H01[e];
+      W[e] = h;
+      W[NN + e] = h;
+      W[2 * NN + e] = h;
+      W[3 * NN + e] = H01[e];
       const int i = e % N, j = e / N;
       const double2 t = H01[j + (size_t)i * N];
-      Be[e] = make_double2(t.x, -t.y);
+      W[4 * NN + e] = make_double2(t.x, -t.y);
     }
     __syncthreads();
-
-    int st = 0, it = 0;
-    bool conv = false;
-    for (int itc = 1; itc <= a.itermax; ++itc) {              // src/surfgreen.f90:86
-      it = itc;
-      if (invert(E, G)) st |= PT_SINGULAR;                    // :88-89
-      __syncthreads();
-      cta_gemm<RP, EPI_STORE>(Al, G, N, a.KC, s.sX, s.sY, M1, nullptr);    // :92
-      cta_gemm<RP, EPI_STORE>(Be, G, N, a.KC, s.sX, s.sY, M2, nullptr);    // :95
-      cta_gemm<RP, EPI_ADD2>(M1, Be, N, a.KC, s.sX, s.sY, E, ES);          // :98-102
-      cta_gemm<RP, EPI_ADD2>(M2, Al, N, a.KC, s.sX, s.sY, E, ET);          // :107-110
-      double part = cta_gemm<RP, EPI_STORE_NORM>(M1, Al, N, a.KC, s.sX, s.sY, G, nullptr);  // :113
-      cta_gemm<RP, EPI_STORE>(M2, Be, N, a.KC, s.sX, s.sY, M1, nullptr);   // :116
-      // rotate buffers: alpha <- G, beta <- M1
-      double2* t0 = Al;
-      Al = G;
-      G = t0;
-      double2* t1 = Be;
-      Be = M1;
-      M1 = t1;
-      const double nrm = block_sum(part, s);                  // :120
-      if (nrm <= a.tol) {                                     // :121
-        conv = true;
-        break;
-      }
-    }
-    if (!conv) st |= PT_NOT_CONVERGED;
-
     const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
-    double dl = 0.0, dr = 0.0, db = 0.0;
-    // GLL = (w - eps_s)^-1                                   // :127-128
-    if (invert(ES, a.gll ? a.gll + (size_t)inst * NN : nullptr)) st |= PT_SINGULAR;
-    double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    fp64_solve<RP, GI>(N, a.KC, w, a, a.gll ? a.gll + (size_t)inst * NN : nullptr,
+                       a.grr ? a.grr + (size_t)inst * NN : nullptr,
+                       a.gb ? a.gb + (size_t)inst * NN : nullptr, W, s,
+                       [&](double dl, double dr, double db, const double* spin, int it, int st) {
+                         a.dos_l[oidx] = dl;
+                         a.dos_r[oidx] = dr;
+                         a.dos_bulk[oidx] = db;
+                         if (a.spin[0])
+                           for (int c = 0; c < 6; ++c) a.spin[c][oidx] = spin[c];
+                         if (a.iters) a.iters[oidx] = it;
+                         if (a.status) a.status[oidx] = (uint8_t)st;
+                       });
+  }
+}
+
+// Uneven batch: points of several models (different Ndim, eta per point) in
+// one persistent launch.  CTAs take points in the host's cost order (largest
+// first); each point runs its own Fourier sum, then the shared-memory or the
+// global-memory inverse variant by its Ndim, and stops at its own convergence.
+__global__ void __launch_bounds__(256, 1) k_batch_fp64(const __grid_constant__ BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int tid = threadIdx.x;
+  double2* W = a.ws + (size_t)blockIdx.x * a.ws_stride;
+  __shared__ int sinst;
+  for (;;) {
     if (tid == 0) {
-      for (int q = 0; q < a.ntop; ++q) {
-        const int io = a.top[q] - 1;
-        const double v = ginv(io, io).y;
-        dl = a.divide_by_pi ? dl - v / PI_REF : dl - v;
-      }
-      if (a.spin[0])                                          // src/surfstat.f90:162-177
-        spin_sums(ginv, a.nw, a.ntop, a.top, 0,
-                  a.divide_by_pi, spin[0], spin[1], spin[2]);
+      const int q = atomicAdd(a.counter, 1);
+      sinst = q < a.npts ? a.order[q] : -1;
     }
     __syncthreads();
-    // GRR = (w - eps_t)^-1                                   // :130-131
-    if (invert(ET, a.grr ? a.grr + (size_t)inst * NN : nullptr)) st |= PT_SINGULAR;
-    if (tid == 0) {
-      for (int q = 0; q < a.nbot; ++q) {
-        const int io = N - a.nw + a.bot[q] - 1;
-        const double v = ginv(io, io).y;
-        dr = a.divide_by_pi ? dr - v / PI_REF : dr - v;
-      }
-      if (a.spin[0]) {                                        // src/surfstat.f90:178-192
-        if (a.spin_right_bottom)                              // src/fermiarc.f90:300-327
-          spin_sums(ginv, a.nw, a.nbot, a.bot, N - a.nw, a.divide_by_pi, spin[3], spin[4], spin[5]);
-        else
-          spin_sums(ginv, a.nw, a.ntop, a.top, 0, a.divide_by_pi, spin[3], spin[4], spin[5]);
-      }
-    }
+    const int p = sinst;
     __syncthreads();
-    // GB = (w - eps)^-1                                      // :133-134
-    if (invert(E, a.gb ? a.gb + (size_t)inst * NN : nullptr)) st |= PT_SINGULAR;
-    if (tid == 0) {
-      for (int i = 0; i < N; ++i) {
-        const double v = ginv(i, i).y;
-        db = a.divide_by_pi ? db - v / PI_REF : db - v;
-      }
-      if (!isfinite(dl) || !isfinite(dr) || !isfinite(db)) st |= PT_NONFINITE;
-      a.dos_l[oidx] = dl;
-      a.dos_r[oidx] = dr;
-      a.dos_bulk[oidx] = db;
-      if (a.spin[0])
-        for (int c = 0; c < 6; ++c) a.spin[c][oidx] = spin[c];
-      if (a.iters) a.iters[oidx] = it;
-      if (a.status) a.status[oidx] = (uint8_t)st;
-    }
-    __syncthreads();
+    if (p < 0) break;
+    const BatchModel& m = a.models[a.pmodel[p]];
+    const int N = m.N;
+    const bool gi = N > a.smem_gj_max;
+    const Shared s = fp64_layout(smraw, N, a.KC, !gi);
+    fourier_fill(m, a.k[p], a.k[p + a.npts], W, reinterpret_cast<double2*>(smraw + a.ph_off));
+    SolveOpts o;
+    o.nw = m.nw;
+    o.tol = a.tol;
+    o.itermax = a.itermax;
+    o.divide_by_pi = a.divide_by_pi;
+    o.ntop = m.ntop;
+    o.nbot = m.nbot;
+    o.top = m.top;
+    o.bot = m.bot;
+    for (int c = 0; c < 6; ++c) o.spin[c] = nullptr;
+    o.spin_right_bottom = 0;
+    const double2 w = make_double2(a.omega[p], a.eta[p]);
+    auto emit = [&](double dl, double dr, double db, const double*, int it, int st) {
+      a.dos_l[p] = dl;
+      a.dos_r[p] = dr;
+      a.dos_bulk[p] = db;
+      if (a.iters) a.iters[p] = it;
+      if (a.status) a.status[p] = (uint8_t)st;
+    };
+    if (gi) fp64_solve<13, true>(N, a.KC, w, o, nullptr, nullptr, nullptr, W, s, emit);
+    else fp64_solve<13, false>(N, a.KC, w, o, nullptr, nullptr, nullptr, W, s, emit);
   }
 }
 
@@ -267,6 +344,49 @@ cudaError_t launch_decimate_fp64(const DecimArgs& a, const DecimConfig& cfg, int
     case 8: k_decimate_fp64<8, false><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
     default: k_decimate_fp64<13, false><<<grid, cfg.threads, cfg.smem, s>>>(a); break;
   }
+  return cudaGetLastError();
+}
+
+size_t batch_ws_matrices(int precision_mixed) { return precision_mixed ? 11 : 9; }
+
+static size_t batch_fp64_smem(int max_n, int max_smem_gj_n, int KC) {
+  size_t b = smem_bytes(max_n, KC, false);
+  if (max_smem_gj_n > 0) {
+    const size_t t = smem_bytes(max_smem_gj_n, KC, true);
+    if (t > b) b = t;
+  }
+  return b;
+}
+
+cudaError_t batch_fp64_config(int max_n, size_t extra_smem, int* smem_gj_max, DecimConfig* cfg) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int smem_optin = 0;
+  e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if (max_n > decim_fp64_large_max_n()) return cudaErrorInvalidValue;
+  const int KC = 16;
+  // the shared-memory inverse up to the largest Ndim that fits beside the stages
+  int g = 0;
+  while (g + 1 <= decim_fp64_max_n() && smem_bytes(g + 1, KC, true) + extra_smem + 16 <= (size_t)smem_optin)
+    ++g;
+  *smem_gj_max = g;
+  cfg->threads = 256;
+  cfg->KC = KC;
+  cfg->RP = 13;
+  cfg->inv_global = 1;
+  cfg->smem = batch_fp64_smem(max_n, std::min(g, max_n), KC);
+  if (cfg->smem + extra_smem + 16 > (size_t)smem_optin) return cudaErrorInvalidValue;
+  cfg->ctas_per_sm = 1;
+  return cudaSuccess;
+}
+
+cudaError_t launch_batch_fp64(const BatchArgs& a, const DecimConfig& cfg, int grid, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_batch_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)cfg.smem);
+  if (e != cudaSuccess) return e;
+  k_batch_fp64<<<grid, cfg.threads, cfg.smem, s>>>(a);
   return cudaGetLastError();
 }
 

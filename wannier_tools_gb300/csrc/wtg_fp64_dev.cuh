@@ -426,3 +426,36 @@ __device__ double block_sum(double v, const Shared& s) {
   return t;
 }
 
+// H00 / H01 of one in-plane k point straight into workspace matrices 0..4
+// (eps, eps_s, eps_t = H00; alpha = H01; beta = H01^dagger).  Each entry is
+// the same sum, in the same R order with the same phases, as k_fourier's
+// (src/ham_qlayer2qlayer.f90:45-87); ph is a shared-memory table of nRu phases.
+__device__ void fourier_fill(const BatchModel& m, double k1, double k2, double2* W,
+                             double2* __restrict__ ph) {
+  const int N = m.N, NN = N * N, nw = m.nw, nw2 = nw * nw, T = blockDim.x, tid = threadIdx.x;
+  for (int r = tid; r < m.nRu; r += T) {
+    const double kdotr = k1 * m.rab[r].x + k2 * m.rab[r].y;  // :55
+    double sn, cs;
+    sincos(2.0 * PI_REF * kdotr, &sn, &cs);                   // :56
+    ph[r] = make_double2(cs, sn);
+  }
+  __syncthreads();
+  for (int e = tid; e < NN; e += T) {
+    const int i = e % N, j = e / N;
+    const int bi = i / nw, ie = i % nw, bj = j / nw, je = j % nw;
+    const int el = ie + je * nw;
+    double2 v0 = make_double2(0.0, 0.0), v1 = v0;
+    const int g0 = bj - bi - m.ic_lo;                         // H00 block (bi, bj): ic = bj - bi
+    if (g0 >= 0 && g0 < m.nic)
+      for (int r = m.icoff[g0]; r < m.icoff[g0 + 1]; ++r) cfma(v0, m.hr[(size_t)r * nw2 + el], ph[r]);
+    const int g1 = bj + m.np - bi - m.ic_lo;                  // H01 block (bi, bj): ic = bj + Np - bi
+    if (g1 >= 0 && g1 < m.nic)
+      for (int r = m.icoff[g1]; r < m.icoff[g1 + 1]; ++r) cfma(v1, m.hr[(size_t)r * nw2 + el], ph[r]);
+    W[e] = v0;
+    W[NN + e] = v0;
+    W[2 * NN + e] = v0;
+    W[3 * NN + e] = v1;
+    W[4 * NN + j + (size_t)i * N] = make_double2(v1.x, -v1.y);
+  }
+  __syncthreads();
+}

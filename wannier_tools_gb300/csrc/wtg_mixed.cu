@@ -5,33 +5,35 @@
 //   * each FP64 operand is written as 49-bit fixed point against a shared
 //     exponent per row (left factor) or per column (right factor) and cut into
 //     seven 7-bit digits; a digit is an exact BF16 value (with a power-of-two
-//     scale folded in);
+//     scale folded in), made by one FFMA from the digit's integer bits;
 //   * slice products A^p B^q with p + q <= 8 are issued as BF16 MMAs with FP32
 //     accumulators in tensor memory, one accumulator per slice order
-//     t = p + q for t = 2, 3, 4, 5 (sums of at most 4 * 2K digit products stay
-//     below 2^24, where the tensor core's accumulation is exact) and one for
+//     t = p + q for t = 2, 3, 4, 5 (sums of at most 4 * 127^2 * K digit
+//     products stay below 2^24, where the tensor core's accumulation is exact;
+//     above K = 256 order 5 takes two accumulators, one per K half) and one for
 //     t >= 6 (its accumulation truncates; at 2^-28 of the result that costs
 //     ~2^-44);  49 bits are needed because the Newton-Schulz refinement below
 //     can only be as accurate as its residual product;
-//   * the four accumulators are read back (tcgen05.ld), converted to integers
-//     and summed in int64, and the FP64 result is assembled with integer
+//   * the accumulators are read back (tcgen05.ld), converted to integers and
+//     summed in int64, and the FP64 result is assembled with integer
 //     operations (no FP64 arithmetic for the product itself).
-// The complex product runs in passes: Cr = Xr Yr - Xi Yi (the second term via
-// the instruction's negate-B bit) and Ci = Xr Yi + Xi Yr, each over all output
-// columns when five accumulators fit in the 512 tensor-memory columns
-// (Ndim <= 96) and over two column halves otherwise.  Digits become BF16 bits
-// through per-slice lookup tables in shared memory.
-// Inverses (zgesv with identity, src/inverse.f90:43-55) are a shared-memory
-// FP32 Gauss-Jordan followed by Newton-Schulz refinement X <- X + X (I - M X)
-// whose two products are the split products above, so the inverse reaches the
-// products' accuracy.  Convergence test sum |alpha_ij| (src/surfgreen.f90:120)
-// is evaluated in FP32 from the assembled values.
+// The complex product runs in passes over row blocks of 128 (the MMA's M):
+// Cr = Xr Yr - Xi Yi (the second term via the instruction's negate-B bit) and
+// Ci = Xr Yi + Xi Yr, both in one pass when their accumulators fit the 512
+// tensor-memory columns (Ndim <= 48), else one component per pass over as many
+// column blocks as the accumulators need (MxPlan).
+// Inverses (zgesv with identity, src/inverse.f90:43-55) are an FP32
+// Gauss-Jordan (shared memory up to Ndim 112, global memory in panels above)
+// followed by Newton-Schulz refinement X <- X + X (I - M X) whose two products
+// are the split products above, so the inverse reaches the products'
+// accuracy.  Convergence test sum |alpha_ij| (src/surfgreen.f90:120) is
+// evaluated in FP32 from the assembled values.
 //
 // Operands are staged per K chunk of 16 (one MMA k-step) into a double-buffered
 // shared-memory area in the canonical K-major, no-swizzle layout (8 x 16-byte
 // core matrices; K-adjacent core matrices 128 B apart, 8-row groups 256 B
-// apart), generated by all threads while the tensor core works on the other
-// buffer; one thread issues the MMAs and commits them to an mbarrier per buffer.
+// apart).  Warps 1..7 generate a chunk's digit planes while warp 0 issues the
+// previous chunk's MMAs (one thread) and commits them to the buffer's mbarrier.
 // Every mbarrier wait is bounded; on a timeout the CTA stops issuing work,
 // marks the instance, waits (bounded) for its MMAs and frees tensor memory.
 #include <cuda_bf16.h>
@@ -66,6 +68,7 @@ constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident c
 // must stay below 2^24.
 struct MxPlan {
   int N, NP, nrb, nacc, both, ncb, w0;
+  int wb;                    // B-plane width of the shared-memory layout (>= w0)
 };
 
 __host__ __device__ inline MxPlan mx_plan(int N) {
@@ -86,6 +89,7 @@ __host__ __device__ inline MxPlan mx_plan(int N) {
       ++p.ncb;
     }
   }
+  p.wb = p.w0;
   return p;
 }
 
@@ -170,15 +174,6 @@ __device__ __forceinline__ unsigned long long fixed49(double x, int E, unsigned&
   return sh < 64 ? (m >> sh) : 0ull;
 }
 
-// BF16 bits of sign * d * 2^s for a 7-bit digit d
-__device__ __forceinline__ uint32_t bf16_digit(uint32_t d, int s, uint32_t neg) {
-  if (d == 0) return 0u;
-  const int L = 31 - __clz(d);
-  const uint32_t mant = (d << (7 - L)) & 0x7Fu;
-  const uint32_t e = (uint32_t)(127 + L + s);
-  return (neg << 15) | (e << 7) | mant;
-}
-
 // integer value of an integer-valued float, divided by 2^7 (truncating):
 // keeps the int64 sum of the slice-order accumulators below 2^58
 __device__ __forceinline__ long long f2ll_int(uint32_t w) {
@@ -243,8 +238,6 @@ struct MxShared {
   uint64_t* mbar;          // [2]
   uint32_t* tslot;
   int* misc;               // 0 instance, 1 singular, 2 abort
-  uint16_t* lutA;          // [NSL][128] BF16 bits of d * 2^(7(3-p))
-  uint16_t* lutB;          // [NSL][128] BF16 bits of d * 2^(7(5-q))
 };
 
 __host__ __device__ __forceinline__ int bufbytes_of(int WB) {
@@ -253,14 +246,14 @@ __host__ __device__ __forceinline__ int bufbytes_of(int WB) {
 
 // shared-memory layout: two operand buffers (the FP32 Gauss-Jordan matrix
 // aliases them), then the small arrays
-__device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int N, int WB) {
+__device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int WB) {
   MxShared s;
   const int bb = bufbytes_of(WB);
   s.buf[0] = smraw;
   s.buf[1] = smraw + bb;
   s.gj = reinterpret_cast<float2*>(smraw);
   s.pan = reinterpret_cast<float2*>(smraw);
-  s.mult = s.pan + (size_t)N * MX_PANEL;
+  s.mult = s.pan + (size_t)MX_MAXN * MX_PANEL;
   unsigned char* tail = smraw + 2 * bb;
   s.colbuf = reinterpret_cast<float2*>(tail);
   s.rowbuf = s.colbuf + MX_MAXN;
@@ -273,8 +266,6 @@ __device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int N, int W
   s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
   s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
   s.misc = reinterpret_cast<int*>(s.tslot + 2);
-  s.lutA = reinterpret_cast<uint16_t*>(s.misc + 4);
-  s.lutB = s.lutA + NSL * 128;
   return s;
 }
 
@@ -292,14 +283,6 @@ __device__ __forceinline__ void buffer_ready(MxShared& s, MxState& st, int b) {
   }
 }
 
-// fill the digit -> BF16 tables (all threads; a barrier follows before use)
-__device__ __forceinline__ void mx_fill_luts(const MxShared& s) {
-  for (int e = threadIdx.x; e < NSL * 128; e += blockDim.x) {
-    const int p = e >> 7, d = e & 127;
-    s.lutA[e] = (uint16_t)bf16_digit((uint32_t)d, 7 * (3 - (p + 1)), 0u);
-    s.lutB[e] = (uint16_t)bf16_digit((uint32_t)d, 7 * (5 - (p + 1)), 0u);
-  }
-}
 
 // row exponents of X (over re and im), column exponents of Y: biased-exponent
 // maxima by integer max.  Warp w walks columns w, w+8, ... with its lanes on
@@ -339,76 +322,100 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
   __syncthreads();
 }
 
-// digit planes of chunk [k0, k0+16) into buffer b: A = all rows of X,
-// B = columns [jb, jb+width) of Y (as rows of the K-major B^T layout)
-__device__ __forceinline__ uint32_t dig2(const uint16_t* lut, unsigned long long f0,
-                                         unsigned long long f1, int sh, uint32_t n0, uint32_t n1) {
-  const uint32_t d0 = (uint32_t)(f0 >> sh) & 127u, d1 = (uint32_t)(f1 >> sh) & 127u;
-  return ((uint32_t)lut[d0] | (n0 << 15)) | (((uint32_t)lut[d1] | (n1 << 15)) << 16);
+// BF16x2 bits of (d0 * 2^s, d1 * 2^s) for 7-bit digits, signs in sgn (bits 15
+// and 31).  (2^23 + d) * 2^s - 2^(23+s) by one FFMA is d * 2^s exactly, and
+// its low 16 bits are zero, so the BF16 value is the float's upper half.
+__device__ __forceinline__ uint32_t dig2f(uint32_t d0, uint32_t d1, float sc, float off,
+                                          uint32_t sgn) {
+  const float f0 = __fmaf_rn(__uint_as_float(0x4B000000u | d0), sc, off);
+  const float f1 = __fmaf_rn(__uint_as_float(0x4B000000u | d1), sc, off);
+  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632) | sgn;
 }
 
+// digit p (1 = most significant) of a 49-bit value split as hi = bits 21..48, lo = bits 0..20
+template <int P>
+__device__ __forceinline__ uint32_t digit7(uint32_t hi, uint32_t lo) {
+  return P <= 4 ? (hi >> (7 * (4 - P))) & 127u : (lo >> (7 * (7 - P))) & 127u;
+}
+
+// 2^e as a float constant
+__host__ __device__ constexpr float pow2f(int e) {
+  return e >= 0 ? (float)(1ull << (e < 63 ? e : 62)) : 1.0f / (float)(1ull << (-e));
+}
+
+// the seven digit planes (real and imaginary) of one element pair, stored at
+// dst + plane * pstride (words); scale 2^(7 (e0 - p)) for plane p
+template <int E0>
+__device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned long long fr0,
+                                           unsigned long long fr1, unsigned long long fi0,
+                                           unsigned long long fi1, uint32_t sr, uint32_t si) {
+  const uint32_t hr0 = (uint32_t)(fr0 >> 21), lr0 = (uint32_t)fr0 & 0x1FFFFFu;
+  const uint32_t hr1 = (uint32_t)(fr1 >> 21), lr1 = (uint32_t)fr1 & 0x1FFFFFu;
+  const uint32_t hi0 = (uint32_t)(fi0 >> 21), li0 = (uint32_t)fi0 & 0x1FFFFFu;
+  const uint32_t hi1 = (uint32_t)(fi1 >> 21), li1 = (uint32_t)fi1 & 0x1FFFFFu;
+#define WTG_PUT(P)                                                                          \
+  {                                                                                          \
+    constexpr float sc = pow2f(7 * (E0 - P)), off = -pow2f(23 + 7 * (E0 - P));              \
+    dst[(2 * (P - 1)) * pstride] =                                                           \
+        dig2f(digit7<P>(hr0, lr0), digit7<P>(hr1, lr1), sc, off, sr);                        \
+    dst[(2 * (P - 1) + 1) * pstride] =                                                       \
+        dig2f(digit7<P>(hi0, li0), digit7<P>(hi1, li1), sc, off, si);                        \
+  }
+  WTG_PUT(1) WTG_PUT(2) WTG_PUT(3) WTG_PUT(4) WTG_PUT(5) WTG_PUT(6) WTG_PUT(7)
+#undef WTG_PUT
+}
+
+// digit planes of chunk [k0, k0+16) into buffer b: A = rows [rb0, rb0+128) of
+// X, B = columns [jb, jb+width) of Y (as rows of the K-major B^T layout).
+// Work item `it` covers rows (or columns) 8 (it >> 6) + (lane >> 2) and K pair
+// 8 ((it >> 5) & 1) + 2 (lane & 3); in the canonical layout its word sits at
+// byte 4 it of a plane, so each warp store fills one 128-byte core matrix
+// (no bank conflicts).  Generated by threads gtid = 0 .. gthreads-1.
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                            int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b) {
+                            int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b,
+                            int gtid, int gthreads) {
   unsigned char* __restrict__ A = s.buf[b];
   unsigned char* __restrict__ B = A + 2 * NSL * APLANE;
   const int* __restrict__ expA = s.expA;
   const int* __restrict__ expB = s.expB;
-  const uint16_t* __restrict__ lutA = s.lutA;
-  const uint16_t* __restrict__ lutB = s.lutB;
-  const int bplane = WB * KCH * 2;
-  for (int it = threadIdx.x; it < 128 * (KCH / 2); it += blockDim.x) {
-    const int il = it & 127, kk = 2 * (it >> 7), i = rb0 + il;
+  const int bstride = WB * KCH * 2 / 4;           // B plane stride in words
+  for (int it = gtid; it < 128 * (KCH / 2); it += gthreads) {
+    const int cm = it >> 5, ln = it & 31;
+    const int il = (cm >> 1) * 8 + (ln >> 2), kk = (cm & 1) * 8 + (ln & 3) * 2, i = rb0 + il;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(A) + it;
     if (i >= N) {                                  // padding rows of the M = 128 tile
-      const int off = (((il >> 3) * 2 + (kk >> 3)) * 64 + (il & 7) * 8 + (kk & 7)) * 2;
 #pragma unroll
-      for (int pl = 0; pl < 2 * NSL; ++pl) *reinterpret_cast<uint32_t*>(A + pl * APLANE + off) = 0u;
+      for (int pl = 0; pl < 2 * NSL; ++pl) dst[pl * (APLANE / 4)] = 0u;
       continue;
     }
+    const int E = expA[i];
     double2 x0 = make_double2(0.0, 0.0), x1 = x0;
-    int E = 0;
-    if (i < N) {
-      E = expA[i];
-      if (k0 + kk < N) x0 = X[i + (size_t)(k0 + kk) * N];
-      if (k0 + kk + 1 < N) x1 = X[i + (size_t)(k0 + kk + 1) * N];
-    }
+    if (k0 + kk < N) x0 = X[i + (size_t)(k0 + kk) * N];
+    if (k0 + kk + 1 < N) x1 = X[i + (size_t)(k0 + kk + 1) * N];
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(x0.x, E, n0r), f0i = fixed49(x0.y, E, n0i);
     const unsigned long long f1r = fixed49(x1.x, E, n1r), f1i = fixed49(x1.y, E, n1i);
-    const int off = (((il >> 3) * 2 + (kk >> 3)) * 64 + (il & 7) * 8 + (kk & 7)) * 2;
-#pragma unroll
-    for (int p = 1; p <= NSL; ++p) {
-      const int sh = 7 * (NSL - p);
-      const uint16_t* lut = lutA + (p - 1) * 128;
-      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1)) * APLANE + off) = dig2(lut, f0r, f1r, sh, n0r, n1r);
-      *reinterpret_cast<uint32_t*>(A + (2 * (p - 1) + 1) * APLANE + off) = dig2(lut, f0i, f1i, sh, n0i, n1i);
-    }
+    put_digits<3>(dst, APLANE / 4, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
+                  (n0i << 15) | (n1i << 31));
   }
-  for (int it = threadIdx.x; it < width * (KCH / 2); it += blockDim.x) {
-    const int kk = 2 * (it & 7), jl = it >> 3, j = jb + jl;
+  for (int it = gtid; it < width * (KCH / 2); it += gthreads) {
+    const int cm = it >> 5, ln = it & 31;
+    const int jl = (cm >> 1) * 8 + (ln >> 2), kk = (cm & 1) * 8 + (ln & 3) * 2, j = jb + jl;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(B) + it;
     if (j >= N) {                                  // padding columns
-      const int off = (((jl >> 3) * 2 + (kk >> 3)) * 64 + (jl & 7) * 8 + (kk & 7)) * 2;
 #pragma unroll
-      for (int pl = 0; pl < 2 * NSL; ++pl) *reinterpret_cast<uint32_t*>(B + pl * bplane + off) = 0u;
+      for (int pl = 0; pl < 2 * NSL; ++pl) dst[pl * bstride] = 0u;
       continue;
     }
+    const int F = expB[j];
     double2 y0 = make_double2(0.0, 0.0), y1 = y0;
-    int F = 0;
-    if (j < N) {
-      F = expB[j];
-      if (k0 + kk < N) y0 = Y[(k0 + kk) + (size_t)j * N];
-      if (k0 + kk + 1 < N) y1 = Y[(k0 + kk + 1) + (size_t)j * N];
-    }
+    if (k0 + kk < N) y0 = Y[(k0 + kk) + (size_t)j * N];
+    if (k0 + kk + 1 < N) y1 = Y[(k0 + kk + 1) + (size_t)j * N];
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(y0.x, F, n0r), f0i = fixed49(y0.y, F, n0i);
     const unsigned long long f1r = fixed49(y1.x, F, n1r), f1i = fixed49(y1.y, F, n1i);
-    const int off = (((jl >> 3) * 2 + (kk >> 3)) * 64 + (jl & 7) * 8 + (kk & 7)) * 2;
-#pragma unroll
-    for (int q = 1; q <= NSL; ++q) {
-      const int sh = 7 * (NSL - q);
-      const uint16_t* lut = lutB + (q - 1) * 128;
-      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1)) * bplane + off) = dig2(lut, f0r, f1r, sh, n0r, n1r);
-      *reinterpret_cast<uint32_t*>(B + (2 * (q - 1) + 1) * bplane + off) = dig2(lut, f0i, f1i, sh, n0i, n1i);
-    }
+    put_digits<5>(dst, bstride, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
+                  (n0i << 15) | (n1i << 31));
   }
 }
 
@@ -459,7 +466,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
                          MxShared& s, MxState& st) {
   const int N = pl.N, tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
-  const int nacc = pl.nacc, WB = pl.w0;
+  const int nacc = pl.nacc, WB = pl.wb;
   const int npass = pl.both ? 1 : 2 * pl.ncb;
   float nrm = 0.f;
   oz_exponents(X, Y, N, s);
@@ -474,8 +481,10 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
       uint32_t amask = 0u;
       for (int c = 0; c < nch; ++c) {
         const int b = c & 1;
-        buffer_ready(s, st, b);
-        oz_generate(X, Y, N, WB, c * KCH, rb0, jb, width, s, b);
+        if (tid >= 32) {     // warps 1.. generate while warp 0 issues the previous chunk
+          buffer_ready(s, st, b);
+          oz_generate(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32);
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
         st.abort = __syncthreads_or(st.abort);
@@ -939,166 +948,8 @@ __device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int 
   return sing;
 }
 
-__global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const DecimArgs a, int ns_iter,
-                                                            int ns_final) {
-  extern __shared__ __align__(1024) unsigned char smraw[];
-  const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
-  const MxPlan pl = mx_plan(N);
-  MxShared s = mx_layout(smraw, N, pl.w0);
-  mx_fill_luts(s);
-
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[1])));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if ((tid >> 5) == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     saddr(s.tslot)),
-                 "r"(512));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  MxState st;
-  st.tmem = *s.tslot;
-  st.ncommit[0] = st.ncommit[1] = 0;
-  st.nwaited[0] = st.nwaited[1] = 0;
-  st.abort = 0;
-
-  double2* W = a.ws + (size_t)blockIdx.x * 11 * NN;
-  double2* E = W;
-  double2* ES = W + (size_t)NN;
-  double2* ET = W + (size_t)2 * NN;
-  double2* Al = W + (size_t)3 * NN;
-  double2* Be = W + (size_t)4 * NN;
-  double2* G = W + (size_t)5 * NN;
-  double2* M1 = W + (size_t)6 * NN;
-  double2* M2 = W + (size_t)7 * NN;
-  double2* Mi = W + (size_t)8 * NN;
-  double2* R = W + (size_t)9 * NN;
-  double2* Gn = W + (size_t)10 * NN;
-
-  for (;;) {
-    if (tid == 0) s.misc[0] = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int inst = s.misc[0];
-    __syncthreads();
-    if (inst >= a.n_inst || st.abort) break;
-    const int ik = inst / a.nomega, iw = inst % a.nomega;
-    const double2* H00 = a.h + (size_t)ik * 2 * NN;
-    const double2* H01 = H00 + NN;
-    const double2 w = make_double2(a.omega[iw], a.eta);
-    for (int e = tid; e < NN; e += T) {
-      const double2 h = H00[e];
-      E[e] = h;
-      ES[e] = h;
-      ET[e] = h;
-      Al[e] = H01[e];
-      const int i = e % N, j = e / N;
-      const double2 t = H01[j + (size_t)i * N];
-      Be[e] = make_double2(t.x, -t.y);
-    }
-    __syncthreads();
-    int stat = 0, it = 0;
-    bool conv = false;
-    for (int itc = 1; itc <= a.itermax && !st.abort; ++itc) {
-      it = itc;
-      if (mixed_inverse(E, w, pl, ns_iter, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
-      oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);
-      oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st);
-      oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);
-      oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st);
-      const float part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st);
-      oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st);
-      double2* t0 = Al;
-      Al = Gn;
-      Gn = t0;
-      double2* t1 = Be;
-      Be = R;
-      R = t1;
-      const float nrm = block_sum_f(part, s);
-      if ((double)nrm <= a.tol) {
-        conv = true;
-        break;
-      }
-    }
-    if (!conv) stat |= PT_NOT_CONVERGED;
-    const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
-    double dl = 0.0, dr = 0.0, db = 0.0;
-    if (mixed_inverse(ES, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
-    if (a.gll)
-      for (int e = tid; e < NN; e += T) a.gll[(size_t)inst * NN + e] = G[e];
-    double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    if (tid == 0) {
-      for (int q = 0; q < a.ntop; ++q) {
-        const int io = a.top[q] - 1;
-        const double v = G[io + (size_t)io * N].y;
-        dl = a.divide_by_pi ? dl - v / PI_REF : dl - v;
-      }
-      if (a.spin[0])
-        spin_sums([&](int i, int j) { return G[i + (size_t)j * N]; }, a.nw, a.ntop, a.top, 0,
-                  a.divide_by_pi, spin[0], spin[1], spin[2]);
-    }
-    __syncthreads();
-    if (mixed_inverse(ET, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
-    if (a.grr)
-      for (int e = tid; e < NN; e += T) a.grr[(size_t)inst * NN + e] = G[e];
-    if (tid == 0) {
-      for (int q = 0; q < a.nbot; ++q) {
-        const int io = N - a.nw + a.bot[q] - 1;
-        const double v = G[io + (size_t)io * N].y;
-        dr = a.divide_by_pi ? dr - v / PI_REF : dr - v;
-      }
-      if (a.spin[0]) {
-        auto gr = [&](int i, int j) { return G[i + (size_t)j * N]; };
-        if (a.spin_right_bottom)
-          spin_sums(gr, a.nw, a.nbot, a.bot, N - a.nw, a.divide_by_pi, spin[3], spin[4], spin[5]);
-        else
-          spin_sums(gr, a.nw, a.ntop, a.top, 0, a.divide_by_pi, spin[3], spin[4], spin[5]);
-      }
-    }
-    __syncthreads();
-    if (mixed_inverse(E, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
-    if (a.gb)
-      for (int e = tid; e < NN; e += T) a.gb[(size_t)inst * NN + e] = G[e];
-    if (tid == 0) {
-      for (int i = 0; i < N; ++i) {
-        const double v = G[i + (size_t)i * N].y;
-        db = a.divide_by_pi ? db - v / PI_REF : db - v;
-      }
-      if (st.abort) stat |= PT_TIMEOUT;
-      if (!isfinite(dl) || !isfinite(dr) || !isfinite(db)) stat |= PT_NONFINITE;
-      a.dos_l[oidx] = dl;
-      a.dos_r[oidx] = dr;
-      a.dos_bulk[oidx] = db;
-      if (a.spin[0])
-        for (int c = 0; c < 6; ++c) a.spin[c][oidx] = spin[c];
-      if (a.iters) a.iters[oidx] = it;
-      if (a.status) a.status[oidx] = (uint8_t)stat;
-    }
-    __syncthreads();
-  }
-  // drain: every committed MMA must finish before tensor memory is released
-  for (int b = 0; b < 2; ++b)
-    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1);
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  if ((tid >> 5) == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(512));
-}
-
-// single complex product / inverse through the same device code (one CTA)
-__global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const double2* X,
-                                                        const double2* Y, double2* C, double2* ws,
-                                                        int ns, int* status) {
-  extern __shared__ __align__(1024) unsigned char smraw[];
-  const MxPlan pl = mx_plan(N);
-  const int NN = N * N;
-  MxShared s = mx_layout(smraw, N, pl.w0);
-  mx_fill_luts(s);
+// tensor-memory allocation and mbarriers of a CTA (all threads)
+__device__ void mx_setup(MxShared& s, MxState& st) {
   const int tid = threadIdx.x;
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
@@ -1114,11 +965,239 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  MxState st;
   st.tmem = *s.tslot;
   st.ncommit[0] = st.ncommit[1] = 0;
   st.nwaited[0] = st.nwaited[1] = 0;
   st.abort = 0;
+}
+
+// every committed MMA must finish before tensor memory is released
+__device__ void mx_teardown(MxShared& s, MxState& st) {
+  for (int b = 0; b < 2; ++b)
+    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if ((threadIdx.x >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(512));
+}
+
+// Decimation of one instance whose eps, eps_s, eps_t (= H00), alpha (= H01)
+// and beta (= H01^dagger) already sit in workspace matrices 0..4 of W (11
+// N x N matrices); the spectral sums go to emit(dl, dr, db, spin[6],
+// iterations, status) in thread 0, the final inverses to gll / grr / gb when
+// those are not null.  o has DecimArgs' member names (lists, tolerance, ...).
+template <class O, class Emit>
+__device__ void mixed_solve(const MxPlan& pl, double2 w, const O& o, int ns_iter, int ns_final,
+                            double2* gll, double2* grr, double2* gb, double2* W, MxShared& s,
+                            MxState& st, Emit emit) {
+  const int N = pl.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
+  double2* E = W;
+  double2* ES = W + (size_t)NN;
+  double2* ET = W + (size_t)2 * NN;
+  double2* Al = W + (size_t)3 * NN;
+  double2* Be = W + (size_t)4 * NN;
+  double2* G = W + (size_t)5 * NN;
+  double2* M1 = W + (size_t)6 * NN;
+  double2* M2 = W + (size_t)7 * NN;
+  double2* Mi = W + (size_t)8 * NN;
+  double2* R = W + (size_t)9 * NN;
+  double2* Gn = W + (size_t)10 * NN;
+  int stat = 0, it = 0;
+  bool conv = false;
+  for (int itc = 1; itc <= o.itermax && !st.abort; ++itc) {   // src/surfgreen.f90:86-122
+    it = itc;
+    if (mixed_inverse(E, w, pl, ns_iter, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;
+    oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);
+    oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st);
+    oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);
+    oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st);
+    const float part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st);
+    oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st);
+    double2* t0 = Al;
+    Al = Gn;
+    Gn = t0;
+    double2* t1 = Be;
+    Be = R;
+    R = t1;
+    const float nrm = block_sum_f(part, s);
+    if ((double)nrm <= o.tol) {
+      conv = true;
+      break;
+    }
+  }
+  if (!conv) stat |= PT_NOT_CONVERGED;
+  double dl = 0.0, dr = 0.0, db = 0.0;
+  if (mixed_inverse(ES, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;  // :127-128
+  if (gll)
+    for (int e = tid; e < NN; e += T) gll[e] = G[e];
+  double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (tid == 0) {
+    for (int q = 0; q < o.ntop; ++q) {
+      const int io = o.top[q] - 1;
+      const double v = G[io + (size_t)io * N].y;
+      dl = o.divide_by_pi ? dl - v / PI_REF : dl - v;
+    }
+    if (o.spin[0])
+      spin_sums([&](int i, int j) { return G[i + (size_t)j * N]; }, o.nw, o.ntop, o.top, 0,
+                o.divide_by_pi, spin[0], spin[1], spin[2]);
+  }
+  __syncthreads();
+  if (mixed_inverse(ET, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;  // :130-131
+  if (grr)
+    for (int e = tid; e < NN; e += T) grr[e] = G[e];
+  if (tid == 0) {
+    for (int q = 0; q < o.nbot; ++q) {
+      const int io = N - o.nw + o.bot[q] - 1;
+      const double v = G[io + (size_t)io * N].y;
+      dr = o.divide_by_pi ? dr - v / PI_REF : dr - v;
+    }
+    if (o.spin[0]) {
+      auto gr = [&](int i, int j) { return G[i + (size_t)j * N]; };
+      if (o.spin_right_bottom)
+        spin_sums(gr, o.nw, o.nbot, o.bot, N - o.nw, o.divide_by_pi, spin[3], spin[4], spin[5]);
+      else
+        spin_sums(gr, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[3], spin[4], spin[5]);
+    }
+  }
+  __syncthreads();
+  if (mixed_inverse(E, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;   // :133-134
+  if (gb)
+    for (int e = tid; e < NN; e += T) gb[e] = G[e];
+  if (tid == 0) {
+    for (int i = 0; i < N; ++i) {
+      const double v = G[i + (size_t)i * N].y;
+      db = o.divide_by_pi ? db - v / PI_REF : db - v;
+    }
+    if (st.abort) stat |= PT_TIMEOUT;
+    if (!isfinite(dl) || !isfinite(dr) || !isfinite(db)) stat |= PT_NONFINITE;
+    emit(dl, dr, db, spin, it, stat);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const __grid_constant__ DecimArgs a,
+                                                            int ns_iter, int ns_final) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
+  const MxPlan pl = mx_plan(N);
+  MxShared s = mx_layout(smraw, pl.wb);
+  MxState st;
+  mx_setup(s, st);
+  double2* W = a.ws + (size_t)blockIdx.x * 11 * NN;
+  for (;;) {
+    if (tid == 0) s.misc[0] = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int inst = s.misc[0];
+    __syncthreads();
+    if (inst >= a.n_inst || st.abort) break;
+    const int ik = inst / a.nomega, iw = inst % a.nomega;
+    const double2* H00 = a.h + (size_t)ik * 2 * NN;
+    const double2* H01 = H00 + NN;
+    const double2 w = make_double2(a.omega[iw], a.eta);      // src/surfgreen.f90:82
+    for (int e = tid; e < NN; e += T) {                       // :74-78
+      const double2 h = H00[e];
+      W[e] = h;
+      W[NN + e] = h;
+      W[2 * NN + e] = h;
+      W[3 * NN + e] = H01[e];
+      const int i = e % N, j = e / N;
+      const double2 t = H01[j + (size_t)i * N];
+      W[4 * NN + e] = make_double2(t.x, -t.y);
+    }
+    __syncthreads();
+    const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
+    mixed_solve(pl, w, a, ns_iter, ns_final, a.gll ? a.gll + (size_t)inst * NN : nullptr,
+                a.grr ? a.grr + (size_t)inst * NN : nullptr,
+                a.gb ? a.gb + (size_t)inst * NN : nullptr, W, s, st,
+                [&](double dl, double dr, double db, const double* spin, int it, int stat) {
+                  a.dos_l[oidx] = dl;
+                  a.dos_r[oidx] = dr;
+                  a.dos_bulk[oidx] = db;
+                  if (a.spin[0])
+                    for (int c = 0; c < 6; ++c) a.spin[c][oidx] = spin[c];
+                  if (a.iters) a.iters[oidx] = it;
+                  if (a.status) a.status[oidx] = (uint8_t)stat;
+                });
+  }
+  mx_teardown(s, st);
+}
+
+// options of one batch instance, with DecimArgs' member names
+struct MxOpts {
+  int nw;
+  double tol;
+  int itermax;
+  int divide_by_pi;
+  int ntop, nbot;
+  const int* top;
+  const int* bot;
+  double* spin[6];
+  int spin_right_bottom;
+};
+
+// Uneven batch in one persistent launch (mixed form): as k_batch_fp64, with the
+// shared-memory layout sized for the widest B plane of the batch (a.wb).
+__global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__ BatchArgs a,
+                                                         int ns_iter, int ns_final) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  const int tid = threadIdx.x;
+  MxShared s = mx_layout(smraw, a.wb);
+  MxState st;
+  mx_setup(s, st);
+  double2* W = a.ws + (size_t)blockIdx.x * a.ws_stride;
+  for (;;) {
+    if (tid == 0) {
+      const int q = atomicAdd(a.counter, 1);
+      s.misc[0] = q < a.npts ? a.order[q] : -1;
+    }
+    __syncthreads();
+    const int p = s.misc[0];
+    __syncthreads();
+    if (p < 0 || st.abort) {
+      if (p >= 0 && tid == 0 && a.status) a.status[p] = PT_TIMEOUT;
+      if (p < 0) break;
+      continue;
+    }
+    const BatchModel& m = a.models[a.pmodel[p]];
+    MxPlan pl = mx_plan(m.N);
+    pl.wb = a.wb;
+    fourier_fill(m, a.k[p], a.k[p + a.npts], W, reinterpret_cast<double2*>(smraw + a.ph_off));
+    MxOpts o;
+    o.nw = m.nw;
+    o.tol = a.tol;
+    o.itermax = a.itermax;
+    o.divide_by_pi = a.divide_by_pi;
+    o.ntop = m.ntop;
+    o.nbot = m.nbot;
+    o.top = m.top;
+    o.bot = m.bot;
+    for (int c = 0; c < 6; ++c) o.spin[c] = nullptr;
+    o.spin_right_bottom = 0;
+    mixed_solve(pl, make_double2(a.omega[p], a.eta[p]), o, ns_iter, ns_final, nullptr, nullptr,
+                nullptr, W, s, st,
+                [&](double dl, double dr, double db, const double*, int it, int stat) {
+                  a.dos_l[p] = dl;
+                  a.dos_r[p] = dr;
+                  a.dos_bulk[p] = db;
+                  if (a.iters) a.iters[p] = it;
+                  if (a.status) a.status[p] = (uint8_t)stat;
+                });
+  }
+  mx_teardown(s, st);
+}
+
+// single complex product / inverse through the same device code (one CTA)
+__global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const double2* X,
+                                                        const double2* Y, double2* C, double2* ws,
+                                                        int ns, int* status) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  const MxPlan pl = mx_plan(N);
+  const int NN = N * N;
+  MxShared s = mx_layout(smraw, pl.wb);
+  const int tid = threadIdx.x;
+  MxState st;
+  mx_setup(s, st);
   int sing = 0;
   if (op == 0) {
     oz_gemm<OZ_STORE>(X, Y, pl, C, nullptr, nullptr, s, st);
@@ -1133,26 +1212,20 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
                          ws + 3 * (size_t)NN, s, st);
     for (int e = tid; e < NN; e += blockDim.x) C[e] = G[e];
   }
-  for (int b = 0; b < 2; ++b)
-    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1);
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
   if (tid == 0) *status = (st.abort ? PT_TIMEOUT : 0) | (sing ? PT_SINGULAR : 0);
-  if ((tid >> 5) == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(st.tmem), "r"(512));
+  mx_teardown(s, st);
 }
 
-size_t mixed_smem(int N) {
+size_t mixed_smem(int N, int wb = 0) {
   const MxPlan pl = mx_plan(N);
-  const size_t bufbytes = (size_t)bufbytes_of(pl.w0);
+  const size_t bufbytes = (size_t)bufbytes_of(wb > 0 ? wb : pl.w0);
   // the FP32 Gauss-Jordan matrix ((N+1)*N float2, Ndim <= MX_SMEM_GJ_N) or the
   // panel and multiplier columns (2 * N * MX_PANEL float2) alias the buffers
   size_t planes = 2 * bufbytes;
-  const size_t gj = N <= MX_SMEM_GJ_N ? (size_t)(N + 1) * N * 8 : (size_t)2 * N * MX_PANEL * 8;
+  const size_t gj = N <= MX_SMEM_GJ_N ? (size_t)(N + 1) * N * 8 : (size_t)2 * MX_MAXN * MX_PANEL * 8;
   if (gj > planes) planes = gj;
   return planes + (size_t)MX_MAXN * 8 * 2 + MX_PANEL * 8 + (size_t)MX_MAXN * 4 * 4 + 32 * 4 +
-         16 + 8 + 16 + 2 * NSL * 128 * 2;
+         16 + 8 + 16;
 }
 
 }  // namespace
@@ -1180,6 +1253,34 @@ cudaError_t decim_mixed_config(int N, DecimConfig* cfg) {
 cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                   cudaStream_t s) {
   k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 6, 8);
+  return cudaGetLastError();
+}
+
+cudaError_t batch_mixed_config(int max_n, int* wb, DecimConfig* cfg) {
+  if (max_n > MX_MAXN) return cudaErrorInvalidValue;
+  int w = 16;
+  size_t smem = 0;
+  for (int n = 1; n <= max_n; ++n) w = w > mx_plan(n).w0 ? w : mx_plan(n).w0;
+  for (int n = 1; n <= max_n; ++n) {
+    const size_t t = mixed_smem(n, w);
+    smem = smem > t ? smem : t;
+  }
+  *wb = w;
+  cfg->threads = MX_T;
+  cfg->KC = 0;
+  cfg->RP = 0;
+  cfg->inv_global = 0;
+  cfg->smem = smem > (size_t)(116 << 10) ? smem : (size_t)(116 << 10);
+  cfg->ctas_per_sm = 1;
+  return cudaSuccess;
+}
+
+cudaError_t launch_batch_mixed(const BatchArgs& a, const DecimConfig& cfg, int grid,
+                               cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_batch_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)cfg.smem);
+  if (e != cudaSuccess) return e;
+  k_batch_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 6, 8);
   return cudaGetLastError();
 }
 
