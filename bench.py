@@ -58,6 +58,21 @@ WORKLOADS = {
                         "101 k x 201 omega in [-1,1] eV, eta=1e-2 eV, tol=1e-10, FP64"),
     # the large k-path x omega spectrum: 301 k x 501 omega at Ndim 264; one k point
     # (501 solves) per step, a strided subset of omegas in the CPU sample
+    # four models of Ndim 16, 40, 112, 264 interleaved in one persistent launch per step; each
+    # model has 4096 random (k, omega) points, eta log-uniform in [1e-4, 1e-2] eV; a step is 256
+    # points of each model (the next slice of the 4 x 4096 set)
+    "uneven4": dict(kind="uneven", shapes=[(8, 2), (20, 2), (56, 2), (88, 3)], seed=2027,
+                    per_model=4096, step_per_model=256, cpu_per_model=16,
+                    desc="uneven batch: synthetic models of Ndim 16/40/112/264 (Num_wann/Np "
+                         "8/2, 20/2, 56/2, 88/3) interleaved in one persistent launch, 4096 "
+                         "random (k,omega) each, eta log-uniform [1e-4,1e-2] eV"),
+    # request loop: 8 models (Ndim 8..300), Poisson arrivals, requests of 50-400 points
+    "serve8": dict(kind="serve", shapes=[(8, 1), (16, 2), (30, 2), (40, 3), (56, 2), (75, 2),
+                                         (88, 3), (150, 2)], seed=2028, requests=24,
+                   rates=(2.0, 8.0, 32.0), slot_points=512, slots=4,
+                   desc="serving loop: 8 synthetic models Num_wann 8..150, Np 1..3 (Ndim 8..300), "
+                        "Poisson requests of 50-400 (k,omega) points, random omega windows in "
+                        "[-1,1] eV, eta log-uniform [1e-3,1e-2] eV"),
     "ss_n264": dict(nw=88, np_=3, seed=2026, nk1=301, nk2=None, omega_ev=None, eta_ev=1e-3,
                     divide_by_pi=False, tol=None, cpu_per_core=1, ref_per_core=1,
                     omega_range=(-0.5, 0.5), nomega=501, step_k=1, cpu_omegas=6,
@@ -472,6 +487,189 @@ def run_reference(args):
         dist.destroy_process_group()
 
 
+def _uneven_points(wl):
+    import numpy as np
+    rng = np.random.default_rng(wl["seed"])
+    nm, per = len(wl["shapes"]), wl["per_model"]
+    k = rng.uniform(-0.5, 0.5, (nm, per, 2))
+    om = rng.uniform(-1.0, 1.0, (nm, per)) * EV2HARTREE
+    eta = np.exp(rng.uniform(np.log(1e-4), np.log(1e-2), (nm, per))) * EV2HARTREE
+    return k, om, eta
+
+
+def _uneven_step(wl, step):
+    """Points of one step: the step-th slice of step_per_model points of every model, interleaved."""
+    import numpy as np
+    k, om, eta = _uneven_points(wl)
+    nm, sp, per = len(wl["shapes"]), wl["step_per_model"], wl["per_model"]
+    idx = (np.arange(sp) + step * sp) % per
+    pm = np.tile(np.arange(nm, dtype=np.int32), sp)
+    ii = np.repeat(idx, nm)
+    return pm, k[pm, ii], om[pm, ii], eta[pm, ii]
+
+
+def _uneven_cpu_worker(args):
+    import numpy as np
+    from oracle import wt_oracle as O
+    from wannier_tools_gb300 import synthetic
+    (nw, np_, seed), kk, om, eta = args
+    m = synthetic.make_model(nw, np_, seed=seed)
+    allorb = list(range(1, nw + 1))
+    t0 = time.perf_counter()
+    r = O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, nw, np_, np.asarray([kk]), np.asarray([om]),
+                           eta, allorb, allorb)
+    return time.perf_counter() - t0, (float(r["dos_l"][0, 0]), float(r["dos_r"][0, 0]),
+                                      float(r["dos_bulk"][0, 0]))
+
+
+def run_uneven(args):
+    """One persistent launch per step over points of four models of different Ndim."""
+    import numpy as np
+    import torch
+
+    import wannier_tools_gb300 as w
+    from wannier_tools_gb300 import api
+    from wannier_tools_gb300._lib import PREC_FP64, PREC_MIXED
+
+    wl = WORKLOADS[args.workload]
+    ncores = os.cpu_count() or 1
+    pool = None if args.no_cpu_baseline else cpu_pool(ncores)
+    w.build()
+    torch.cuda.set_device(0)
+    ms = [w.make_model(nw, np_, seed=wl["seed"] + i) for i, (nw, np_) in enumerate(wl["shapes"])]
+    gs = [w.Model.from_surface_model(m) for m in ms]
+    tops = [list(range(1, m.nw + 1)) for m in ms]
+    npts = len(wl["shapes"]) * wl["step_per_model"]
+    precs = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+    forms = [args.precision] + ([] if args.only else [f for f in ("fp64", "mixed") if f != args.precision])
+    res = {}
+    for f in forms:
+        with api.Engine(gs, tops, tops, precision=precs[f], max_points=npts) as eng:
+            for i in range(args.warmup):
+                eng.run(*_uneven_step(wl, i))
+            steps = [_uneven_step(wl, args.warmup + i) for i in range(args.steps)]
+            l0 = eng.info()["launches"]
+            with ClockSampler(0) as clk:
+                t0 = time.perf_counter()
+                outs = [eng.run(*st) for st in steps]
+                dt = time.perf_counter() - t0
+            n3 = np.array([float(m.ndim) ** 3 for m in ms])
+            its = np.concatenate([o["iters"] for o in outs])
+            pms = np.concatenate([st[0] for st in steps])
+            res[f] = {"value": len(pms) / dt, "ms": 1e3 * dt / args.steps, "clocks": clk.summary(),
+                      "its": its, "flagged": int(sum((o["status"] != 0).sum() for o in outs)),
+                      "fp64_flops": float(((56.0 * its + 24.0) * n3[pms]).sum()), "dt": dt,
+                      "launches": eng.info()["launches"] - l0, "first": (steps[0], outs[0])}
+    cpu, errs = None, {}
+    if pool is not None:
+        # bounded oracle sample: cpu_per_model points of each model from the first timed step
+        (pm, k, om, eta), _ = res[forms[0]]["first"]
+        sel = np.concatenate([np.where(pm == i)[0][:wl["cpu_per_model"]] for i in range(len(ms))])
+        tasks = [((wl["shapes"][pm[j]][0], wl["shapes"][pm[j]][1], wl["seed"] + int(pm[j])), k[j],
+                  om[j], eta[j]) for j in sel]
+        pool.map(_cpu_warm, [WORKLOADS["ss_n40"]] * ncores, chunksize=1)
+        t0 = time.perf_counter()
+        rs = pool.map(_uneven_cpu_worker, tasks, chunksize=1)
+        wall = time.perf_counter() - t0
+        pool.close()
+        cpu = {"value": len(sel) / wall, "unit": "solves/s", "cores": ncores, "kind": "port",
+               "sample": f"{len(sel)} points ({wl['cpu_per_model']} per model) of the first timed "
+                         f"step, {ncores} spawned processes x 1 OpenBLAS thread, {wall:.1f} s wall"}
+        ref = np.array([r[1] for r in rs])
+        for f in forms:
+            o = res[f]["first"][1]
+            got = np.stack([o["dos_l"][sel], o["dos_r"][sel], o["dos_bulk"][sel]], 1)
+            e = np.abs(got - ref) / np.abs(ref)
+            errs[f] = {"dos_l": float(e[:, 0].max()), "dos_r": float(e[:, 1].max()),
+                       "dos_bulk": float(e[:, 2].max()), "points": int(len(sel))}
+    r = res[forms[0]]
+    line = {"metric": METRIC, "value": r["value"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["desc"], "points_per_step": npts, "precision": forms[0],
+                       "launch": "one persistent k_batch launch per step, points in cost order",
+                       "timing": "wall clock around wtg_engine_run (host inputs, host outputs)",
+                       "l2": "inputs larger than L2: 152 workspaces of 9-11 x 264^2 complex",
+                       "mean_iterations": float(r["its"].mean()), "status_flagged_points": r["flagged"]},
+            "e2e": {"value": r["value"], "unit": "solves/s", "h2d_bytes_per_step": npts * 40,
+                    "d2h_bytes_per_step": npts * 29},
+            "gpu_launches": r["launches"],
+            "fp64_equivalent_tflops": r["fp64_flops"] / r["dt"] / 1e12,
+            "clocks": r["clocks"], "cpu_baseline": cpu, "max_rel_err_vs_fp64_oracle": errs.get(forms[0])}
+    for f in forms[1:]:
+        o = res[f]
+        line[f] = {"value": o["value"], "ms_per_step": o["ms"], "speedup_vs_" + forms[0]: o["value"] / r["value"],
+                   "fp64_equivalent_tflops": o["fp64_flops"] / o["dt"] / 1e12,
+                   "mean_iterations": float(o["its"].mean()), "status_flagged_points": o["flagged"],
+                   "max_rel_err_vs_fp64_oracle": errs.get(f), "clocks": o["clocks"]}
+    print(json.dumps(line))
+    for g in gs:
+        g.close()
+
+
+def run_serve(args):
+    """Poisson request streams through the continuous-batching loop at swept rates."""
+    import numpy as np
+    import torch
+
+    import wannier_tools_gb300 as w
+    from wannier_tools_gb300._lib import PREC_FP64, PREC_MIXED
+    from wannier_tools_gb300.serving import SurfaceServer, poisson_requests, replay
+
+    wl = WORKLOADS[args.workload]
+    w.build()
+    torch.cuda.set_device(0)
+    ms = [w.make_model(nw, np_, seed=wl["seed"] + i) for i, (nw, np_) in enumerate(wl["shapes"])]
+    gs = [w.Model.from_surface_model(m) for m in ms]
+    tops = [list(range(1, m.nw + 1)) for m in ms]
+    precs = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+    forms = [args.precision] + ([] if args.only else [f for f in ("fp64", "mixed") if f != args.precision])
+    out = {}
+    for f in forms:
+        sweep = []
+        with SurfaceServer(gs, tops, tops, precision=precs[f], slot_points=wl["slot_points"],
+                           max_slots=wl["slots"]) as srv:
+            warm = poisson_requests(np.random.default_rng(1), len(ms), 1e3, max(3, args.warmup))
+            replay(srv, warm, EV2HARTREE)
+            l0 = sum(e.info()["launches"] for e in srv.engines)
+            with ClockSampler(0) as clk:
+                for i, rate in enumerate(wl["rates"]):
+                    reqs = poisson_requests(np.random.default_rng(wl["seed"] + i), len(ms), rate,
+                                            wl["requests"])
+                    rep = replay(srv, reqs, EV2HARTREE)
+                    rep.pop("results")
+                    rep["rate_per_s"] = rate
+                    sweep.append(rep)
+            launches = sum(e.info()["launches"] for e in srv.engines) - l0
+            nslots = len(srv.engines)
+        out[f] = {"sweep": sweep, "clocks": clk.summary(), "launches": launches, "slots": nslots}
+    r = out[forms[0]]
+    best = max(r["sweep"], key=lambda x: x["solves_per_s"])
+    line = {"metric": METRIC, "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "steps": len(r["sweep"]), "warmup": max(3, args.warmup),
+            "ms_per_step": 1e3 * sum(x["wall_s"] for x in r["sweep"]) / len(r["sweep"]),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": wl["desc"], "precision": forms[0], "slots": r["slots"],
+                       "slot_points": wl["slot_points"], "requests_per_rate": wl["requests"],
+                       "step": "one Poisson replay at one rate; value = best served solves/s",
+                       "timing": "wall clock from first arrival to last completion"},
+            "latency_ms": {"p50": best["p50_ms"], "p99": best["p99_ms"], "at_rate_per_s": best["rate_per_s"]},
+            "sweep": r["sweep"],
+            "e2e": {"value": best["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None},
+            "gpu_launches": r["launches"], "clocks": r["clocks"], "cpu_baseline": None}
+    for f in forms[1:]:
+        o = out[f]
+        ob = max(o["sweep"], key=lambda x: x["solves_per_s"])
+        line[f] = {"value": ob["solves_per_s"], "latency_ms": {"p50": ob["p50_ms"], "p99": ob["p99_ms"],
+                                                              "at_rate_per_s": ob["rate_per_s"]},
+                   "sweep": o["sweep"], "clocks": o["clocks"]}
+    print(json.dumps(line))
+    for g in gs:
+        g.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -490,6 +688,15 @@ def main():
                     help="k points per host core per reference-arm step (0 = by workload)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
+    if wl.get("kind") in ("uneven", "serve"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or "
+                              "served form of this path; its CPU arm is timed on arc_n112/ss_n40/ss_n264"}))
+            return
+        if args.warmup < 3:
+            ap.error("--warmup must be >= 3")
+        (run_uneven if wl["kind"] == "uneven" else run_serve)(args)
+        return
     if args.cpu_sample_per_core <= 0:
         args.cpu_sample_per_core = wl["cpu_per_core"]
     if args.ref_per_core <= 0:
