@@ -610,21 +610,94 @@ __device__ __forceinline__ long long cabs1_key_f(float2 v) {
   return (long long)__float_as_uint(fabsf(v.x) + fabsf(v.y));
 }
 
+// pivot over rows >= k of the column values x (rows lane + 32 m): the first
+// maximal |re| + |im| (izamax's rule); warp-uniform result and key
+__device__ __forceinline__ int gj_argmax4(const float2 (&x)[4], int k, int N, long long& best) {
+  const int lane = threadIdx.x & 31;
+  best = -1;
+  int bi = N;
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int i = lane + 32 * m;
+    if (i >= k && i < N) {
+      const long long v = cabs1_key_f(x[m]);
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+  }
+  return bi;
+}
+
+// entry m (warp-uniform) of a 4-entry register column, without local memory
+__device__ __forceinline__ float2 pick4(const float2 (&x)[4], int m) {
+  float2 v = x[0];
+  v = m == 1 ? x[1] : v;
+  v = m == 2 ? x[2] : v;
+  v = m == 3 ? x[3] : v;
+  return v;
+}
+
+__device__ __forceinline__ float2 shfl_f2c(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// step k's pivot data from column k's values x (after step k-1): pivot row,
+// reciprocal, and the multiplier column (column k with rows k and p swapped)
+// into cb; sets misc[1] on an exact zero pivot
+__device__ __noinline__ void gj_pivot_publish(const float2 (&x)[4], int k, int N, float2* cb,
+                                              float2* recip, int* perm, int* misc) {
+  const int lane = threadIdx.x & 31;
+  long long best;
+  const int p = gj_argmax4(x, k, N, best);
+  const float2 xk = shfl_f2c(pick4(x, k >> 5), k & 31);
+  const float2 xp = shfl_f2c(pick4(x, p >> 5), p & 31);
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int i = lane + 32 * m;
+    if (i < N) cb[i] = (i == p) ? xk : x[m];
+  }
+  if (lane == 0) {
+    perm[k] = p;
+    if (best == 0) {
+      misc[1] = 1;
+    } else {
+      const float inv_d = 1.0f / (xp.x * xp.x + xp.y * xp.y);
+      recip[k & 1] = make_float2(xp.x * inv_d, -xp.y * inv_d);
+    }
+  }
+}
+
 // M = w I - X (FP64, kept in Mi for the refinement), then FP32 Gauss-Jordan
 // into G (FP64).  Returns 1 on an exact zero pivot (G = identity then).
+// Ndim <= 112.  Each pivot step is one pass in which every warp takes whole
+// columns into registers (lane l holds rows l, l+32, ...): the row swap, the
+// pivot-row scaling and the elimination of a column happen in registers with
+// two shuffles.  The warp that owns column k+1 also finds step k+1's pivot
+// (look-ahead) and publishes its multiplier column into the other of two
+// buffers, so a step needs one barrier.  Same operations per entry as the
+// step-by-step form.
 __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, double2* Mi,
                           double2* G, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
-  // local copies of the shared-memory pointers (kept in registers)
   float2* __restrict__ sM = s_.gj;
-  float2* __restrict__ colbuf = s_.colbuf;
-  float2* __restrict__ rowbuf = s_.rowbuf;
+  float2* const cb0 = s_.colbuf;          // multiplier columns of even / odd steps
+  float2* const cb1 = s_.rowbuf;
   float2* __restrict__ recip = s_.recip;
   int* __restrict__ perm = s_.perm;
   int* __restrict__ cols = s_.cols;
   int* __restrict__ misc = s_.misc;
-  const int LD = N + 1;                 // odd leading dimension: row walks hit distinct banks
   for (int j = warp; j < N; j += nwarp) {
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
@@ -632,81 +705,59 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
       double2 m = make_double2(-x.x, -x.y);
       if (i == j) m = make_double2(w.x - x.x, w.y - x.y);
       Mi[e] = m;
-      sM[i + j * LD] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+      sM[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
     }
   }
   if (tid == 0) misc[1] = 0;
   __syncthreads();
-  for (int k = 0; k < N; ++k) {
-    if (warp == 0) {
-      long long best = -1;
-      int bi = N;
-      for (int i = k + lane; i < N; i += 32) {
-        const long long v = cabs1_key_f(sM[i + k * LD]);
-        if (v > best) {
-          best = v;
-          bi = i;
-        }
-      }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) {
-          best = ob;
-          bi = oi;
-        }
-      }
-      const int p = bi;
-      for (int i = lane; i < N; i += 32) colbuf[i] = sM[(i == p ? k : i) + k * LD];
-      if (lane == 0) {
-        perm[k] = p;
-        if (best == 0) {
-          misc[1] = 1;
-        } else {
-          const float2 pv = sM[p + k * LD];
-          const float inv_d = 1.0f / (pv.x * pv.x + pv.y * pv.y);
-          recip[0] = make_float2(pv.x * inv_d, -pv.y * inv_d);
-        }
-      }
-    }
-    __syncthreads();
-    if (misc[1]) break;
-    const int p = perm[k];
-    const float2 r = recip[0];
-    for (int j = tid; j < N; j += T) {
-      const float2 akj = sM[k + j * LD];
-      const float2 apj = sM[p + j * LD];
-      if (p != k) sM[p + j * LD] = akj;
-      const float2 nk = (j == k) ? r
-                                 : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
-                                               fmaf(apj.x, r.y, apj.y * r.x));
-      sM[k + j * LD] = nk;
-      rowbuf[j] = nk;
-    }
-    __syncthreads();
-    float2 f[4];                          // this lane's multipliers, rows lane + 32 m
+  if (warp == 0) {                        // step 0's pivot
+    float2 x[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       const int i = lane + 32 * m;
-      f[m] = (i < N && i != k) ? colbuf[i] : make_float2(0.f, 0.f);
+      x[m] = i < N ? sM[i] : make_float2(0.f, 0.f);
+    }
+    gj_pivot_publish(x, 0, N, cb0, recip, perm, misc);
+  }
+  __syncthreads();
+  for (int k = 0; k < N; ++k) {
+    if (misc[1]) break;
+    const int p = perm[k];
+    const float2 r = recip[k & 1];
+    const float2* cb = (k & 1) ? cb1 : cb0;
+    float2* cbn = (k & 1) ? cb0 : cb1;
+    float2 f[4];                          // this lane's multipliers
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = lane + 32 * m;
+      f[m] = i < N ? cb[i] : make_float2(0.f, 0.f);
     }
     for (int j = warp; j < N; j += nwarp) {
-      const float2 rk = rowbuf[j];
-      const bool jk = (j == k);
-      float2* col = sM + j * LD;
+      float2* col = sM + (size_t)j * N;
+      float2 x[4];
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         const int i = lane + 32 * m;
-        if (i < N && i != k) {
-          float2 v = jk ? make_float2(0.f, 0.f) : col[i];
-          v.x = fmaf(-f[m].x, rk.x, v.x);
-          v.x = fmaf(f[m].y, rk.y, v.x);
-          v.y = fmaf(-f[m].x, rk.y, v.y);
-          v.y = fmaf(-f[m].y, rk.x, v.y);
-          col[i] = v;
-        }
+        x[m] = i < N ? col[i] : make_float2(0.f, 0.f);
       }
+      const float2 akj = shfl_f2c(pick4(x, k >> 5), k & 31);
+      const float2 apj = shfl_f2c(pick4(x, p >> 5), p & 31);
+      const bool jk = j == k;
+      const float2 nk = jk ? r
+                           : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
+                                         fmaf(apj.x, r.y, apj.y * r.x));
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int i = lane + 32 * m;
+        float2 v = jk ? make_float2(0.f, 0.f) : ((i == p) ? akj : x[m]);
+        v.x = fmaf(-f[m].x, nk.x, v.x);
+        v.x = fmaf(f[m].y, nk.y, v.x);
+        v.y = fmaf(-f[m].x, nk.y, v.y);
+        v.y = fmaf(-f[m].y, nk.x, v.y);
+        x[m] = (i == k) ? nk : v;
+        if (i < N) col[i] = x[m];
+      }
+      if (j == k + 1) gj_pivot_publish(x, k + 1, N, cbn, recip, perm, misc);
     }
     __syncthreads();
   }
@@ -730,7 +781,7 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
       if (singular) {
         G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
       } else {
-        const float2 v = sM[i + cj * LD];
+        const float2 v = sM[i + (size_t)cj * N];
         G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
       }
     }
@@ -738,7 +789,6 @@ __device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, doubl
   __syncthreads();
   return singular;
 }
-
 
 __device__ __forceinline__ float2 pick_f(const float2 (&x)[MX_ROWS], int m) {
   float2 v = x[0];
