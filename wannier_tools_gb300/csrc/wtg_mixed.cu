@@ -371,6 +371,12 @@ __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned 
 // 8 ((it >> 5) & 1) + 2 (lane & 3); in the canonical layout its word sits at
 // byte 4 it of a plane, so each warp store fills one 128-byte core matrix
 // (no bank conflicts).  Generated by threads gtid = 0 .. gthreads-1.
+// digit planes of chunk [k0, k0+16) into buffer b: A = rows [rb0, rb0+128) of
+// X, B = columns [jb, jb+width) of Y (as rows of the K-major B^T layout).
+// Work item `it` covers rows (or columns) 8 (it >> 6) + (lane >> 2) and K pair
+// 8 ((it >> 5) & 1) + 2 (lane & 3); in the canonical layout its word sits at
+// byte 4 it of a plane, so each warp store fills one 128-byte core matrix
+// (no bank conflicts).  Generated by threads gtid = 0 .. gthreads-1.
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
                             int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b,
                             int gtid, int gthreads) {
@@ -802,20 +808,93 @@ __device__ __forceinline__ float2 shfl_f2(float2 v, int src) {
   return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
+template <int R>
+__device__ __forceinline__ int gj_argmax_r(const float2 (&x)[R], int k, int N, long long& best) {
+  const int lane = threadIdx.x & 31;
+  best = -1;
+  int bi = N;
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    const int i = lane + 32 * m;
+    if (i >= k && i < N) {
+      const long long v = cabs1_key_f(x[m]);
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+  }
+  return bi;
+}
+
+// gj_pivot_publish for a column of MX_ROWS rows per lane; the reciprocal goes to *rslot
+__device__ __noinline__ void gj_pivot_publish_r(const float2 (&x)[MX_ROWS], int k, int N,
+                                                float2* cb, float2* rslot, int* perm, int* misc) {
+  const int lane = threadIdx.x & 31;
+  long long best;
+  const int p = gj_argmax_r<MX_ROWS>(x, k, N, best);
+  const float2 xk = shfl_f2(pick_f(x, k >> 5), k & 31);
+  const float2 xp = shfl_f2(pick_f(x, p >> 5), p & 31);
+#pragma unroll
+  for (int m = 0; m < MX_ROWS; ++m) {
+    const int i = lane + 32 * m;
+    if (i < N) cb[i] = (i == p) ? xk : x[m];
+  }
+  if (lane == 0) {
+    perm[k] = p;
+    if (best == 0) {
+      misc[1] = 1;
+    } else {
+      const float inv_d = 1.0f / (xp.x * xp.x + xp.y * xp.y);
+      *rslot = make_float2(xp.x * inv_d, -xp.y * inv_d);
+    }
+  }
+}
+
+// one Gauss-Jordan step k (pivot row p, reciprocal r, multiplier column cm in
+// shared memory) applied to column j held in registers
+__device__ __forceinline__ void gj_step_col(float2 (&x)[MX_ROWS], const float2* __restrict__ cm,
+                                            int N, int j, int k, int p, float2 r) {
+  const int lane = threadIdx.x & 31;
+  const float2 akj = shfl_f2(pick_f(x, k >> 5), k & 31);
+  const float2 apj = shfl_f2(pick_f(x, p >> 5), p & 31);
+  const bool jk = j == k;
+  const float2 nk = jk ? r : make_float2(fmaf(apj.x, r.x, -apj.y * r.y), fmaf(apj.x, r.y, apj.y * r.x));
+#pragma unroll
+  for (int m = 0; m < MX_ROWS; ++m) {
+    const int i = lane + 32 * m;
+    const float2 f = i < N ? cm[i] : make_float2(0.f, 0.f);
+    float2 v = jk ? make_float2(0.f, 0.f) : ((i == p) ? akj : x[m]);
+    v.x = fmaf(-f.x, nk.x, v.x);
+    v.x = fmaf(f.y, nk.y, v.x);
+    v.y = fmaf(-f.x, nk.y, v.y);
+    v.y = fmaf(-f.y, nk.x, v.y);
+    x[m] = (i == k) ? nk : v;
+  }
+}
+
 // As gj32_start for Ndim above the shared-memory limit: the FP32 matrix lives
 // in global memory (Wf, N x N float2) and the pivot steps run in panels of
-// MX_PANEL columns.  A panel is reduced in shared memory (pivot rows,
-// reciprocals and multiplier columns recorded); then each other column is read
-// once into registers (one warp per column, lane l holding rows l, l+32, ...),
-// put through the panel's steps in order and written back.  Same operations
-// per entry as gj32_start.
+// MX_PANEL columns.  A panel's columns stay in registers (warp w owns panel
+// columns w and w + 8, lane l rows l, l+32, ...); each step updates them with
+// one barrier, the owner of the next column publishing the next pivot and its
+// multiplier column (look-ahead).  Then every other column is read once into
+// registers, put through the panel's steps in order and written back.  Same
+// operations per entry as gj32_start.
 __device__ int gj32_global(const double2* __restrict__ X, double2 w, int N, double2* Mi,
                            double2* G, float2* __restrict__ Wf, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
-  float2* __restrict__ P = s_.pan;
   float2* __restrict__ Cm = s_.mult;
-  float2* __restrict__ rowbuf = s_.rowbuf;
   float2* __restrict__ recip = s_.recip;
   int* __restrict__ perm = s_.perm;
   int* __restrict__ cols = s_.cols;
@@ -834,74 +913,45 @@ __device__ int gj32_global(const double2* __restrict__ X, double2 w, int N, doub
   __syncthreads();
   for (int k0 = 0; k0 < N; k0 += MX_PANEL) {
     const int pb = min(MX_PANEL, N - k0);
-    for (int e = tid; e < N * pb; e += T) P[e] = Wf[(size_t)k0 * N + e];
+    float2 xc[2][MX_ROWS];                // this warp's panel columns warp, warp + nwarp
+#pragma unroll
+    for (int cc = 0; cc < 2; ++cc) {
+      const int c = warp + cc * nwarp;
+#pragma unroll
+      for (int m = 0; m < MX_ROWS; ++m) {
+        const int i = lane + 32 * m;
+        xc[cc][m] = (c < pb && i < N) ? Wf[(size_t)(k0 + c) * N + i] : make_float2(0.f, 0.f);
+      }
+    }
+    if (warp == 0) gj_pivot_publish_r(xc[0], k0, N, Cm, &recip[0], perm, misc);
     __syncthreads();
     for (int t = 0; t < pb; ++t) {
-      const int k = k0 + t;
-      if (warp == 0) {
-        long long best = -1;
-        int bi = N;
-        for (int i = k + lane; i < N; i += 32) {
-          const long long v = cabs1_key_f(P[i + t * N]);
-          if (v > best) {
-            best = v;
-            bi = i;
-          }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) {
-            best = ob;
-            bi = oi;
-          }
-        }
-        const int p = bi;
-        for (int i = lane; i < N; i += 32) Cm[i + t * N] = P[(i == p ? k : i) + t * N];
-        if (lane == 0) {
-          perm[k] = p;
-          if (best == 0) {
-            misc[1] = 1;
-          } else {
-            const float2 pv = P[p + t * N];
-            const float inv_d = 1.0f / (pv.x * pv.x + pv.y * pv.y);
-            recip[t] = make_float2(pv.x * inv_d, -pv.y * inv_d);
-          }
-        }
-      }
-      __syncthreads();
       if (misc[1]) break;
-      const int p = perm[k];
+      const int k = k0 + t, p = perm[k];
       const float2 r = recip[t];
-      if (tid < pb) {
-        const int j = tid;
-        const float2 akj = P[k + j * N];
-        const float2 apj = P[p + j * N];
-        if (p != k) P[p + j * N] = akj;
-        const float2 nk = (j == t) ? r
-                                   : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
-                                                 fmaf(apj.x, r.y, apj.y * r.x));
-        P[k + j * N] = nk;
-        rowbuf[j] = nk;
-      }
-      __syncthreads();
-      for (int e = tid; e < N * pb; e += T) {
-        const int i = e % N, j = e / N;
-        if (i != k) {
-          float2 v = (j == t) ? make_float2(0.f, 0.f) : P[e];
-          const float2 f = Cm[i + t * N];
-          const float2 rk = rowbuf[j];
-          v.x = fmaf(-f.x, rk.x, v.x);
-          v.x = fmaf(f.y, rk.y, v.x);
-          v.y = fmaf(-f.x, rk.y, v.y);
-          v.y = fmaf(-f.y, rk.x, v.y);
-          P[e] = v;
+#pragma unroll
+      for (int cc = 0; cc < 2; ++cc) {
+        const int c = warp + cc * nwarp;
+        if (c < pb) {
+          gj_step_col(xc[cc], Cm + t * N, N, k0 + c, k, p, r);
+          if (c == t + 1) gj_pivot_publish_r(xc[cc], k + 1, N, Cm + (t + 1) * N, &recip[t + 1], perm, misc);
         }
       }
       __syncthreads();
     }
     if (misc[1]) break;
+#pragma unroll
+    for (int cc = 0; cc < 2; ++cc) {       // panel columns back to memory
+      const int c = warp + cc * nwarp;
+      if (c < pb) {
+#pragma unroll
+        for (int m = 0; m < MX_ROWS; ++m) {
+          const int i = lane + 32 * m;
+          if (i < N) Wf[(size_t)(k0 + c) * N + i] = xc[cc][m];
+        }
+      }
+    }
+    // every column outside the panel through the panel's steps, in registers
     for (int j = warp; j < N; j += nwarp) {
       if (j >= k0 && j < k0 + pb) continue;
       float2* col = Wf + (size_t)j * N;
@@ -911,36 +961,13 @@ __device__ int gj32_global(const double2* __restrict__ X, double2 w, int N, doub
         const int i = lane + 32 * q;
         x[q] = i < N ? col[i] : make_float2(0.f, 0.f);
       }
-      for (int t = 0; t < pb; ++t) {
-        const int k = k0 + t, p = perm[k];
-        const float2 r = recip[t];
-        const float2 akj = shfl_f2(pick_f(x, k >> 5), k & 31);
-        const float2 apj = shfl_f2(pick_f(x, p >> 5), p & 31);
-        const float2 nk = make_float2(fmaf(apj.x, r.x, -apj.y * r.y), fmaf(apj.x, r.y, apj.y * r.x));
-        const float2* cm = Cm + t * N;
-#pragma unroll
-        for (int q = 0; q < MX_ROWS; ++q) {
-          const int i = lane + 32 * q;
-          if (i < N && i != k) {
-            float2 v = (i == p) ? akj : x[q];
-            const float2 f = cm[i];
-            v.x = fmaf(-f.x, nk.x, v.x);
-            v.x = fmaf(f.y, nk.y, v.x);
-            v.y = fmaf(-f.x, nk.y, v.y);
-            v.y = fmaf(-f.y, nk.x, v.y);
-            x[q] = v;
-          } else if (i == k) {
-            x[q] = nk;
-          }
-        }
-      }
+      for (int t = 0; t < pb; ++t) gj_step_col(x, Cm + t * N, N, j, k0 + t, perm[k0 + t], recip[t]);
 #pragma unroll
       for (int q = 0; q < MX_ROWS; ++q) {
         const int i = lane + 32 * q;
         if (i < N) col[i] = x[q];
       }
     }
-    for (int e = tid; e < N * pb; e += T) Wf[(size_t)k0 * N + e] = P[e];
     __syncthreads();
   }
   const int singular = misc[1];
@@ -1038,7 +1065,7 @@ __device__ void mx_teardown(MxShared& s, MxState& st) {
 // iterations, status) in thread 0, the final inverses to gll / grr / gb when
 // those are not null.  o has DecimArgs' member names (lists, tolerance, ...).
 template <class O, class Emit>
-__device__ void mixed_solve(const MxPlan& pl, double2 w, const O& o, int ns_iter, int ns_final,
+__device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O& o, int ns_iter, int ns_final,
                             double2* gll, double2* grr, double2* gb, double2* W, MxShared& s,
                             MxState& st, Emit emit) {
   const int N = pl.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
