@@ -174,17 +174,6 @@ __device__ __forceinline__ unsigned long long fixed49(double x, int E, unsigned&
   return sh < 64 ? (m >> sh) : 0ull;
 }
 
-// integer value of an integer-valued float, divided by 2^7 (truncating):
-// keeps the int64 sum of the slice-order accumulators below 2^58
-__device__ __forceinline__ long long f2ll_int(uint32_t w) {
-  const int e = (int)((w >> 23) & 0xFF);
-  if (e < 134) return 0;
-  const long long m = (long long)((w & 0x7FFFFFu) | 0x800000u);
-  const int sh = e - 157;
-  const long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
-  return (w >> 31) ? -v : v;
-}
-
 // double with value S * 2^(be0 - 1023) assembled from bits (truncating)
 __device__ __forceinline__ double assemble(long long S, int be0) {
   if (S == 0) return 0.0;
@@ -295,29 +284,41 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
   int rmax[MX_ROWS];
 #pragma unroll
   for (int m = 0; m < MX_ROWS; ++m) rmax[m] = 0;
-  for (int k = warp; k < N; k += nwarp) {
-    const double2* xc = X + (size_t)k * N;
+  // two columns of X per step so that twice the loads are in flight
+  for (int k = warp; k < N; k += 2 * nwarp) {
+    const double2* xc0 = X + (size_t)k * N;
+    const double2* xc1 = X + (size_t)min(k + nwarp, N - 1) * N;
+    const bool two = k + nwarp < N;
 #pragma unroll
     for (int m = 0; m < MX_ROWS; ++m) {
       const int i = lane + 32 * m;
       if (i < N) {
-        const double2 v = xc[i];
-        rmax[m] = max(rmax[m], max(bexp(v.x), bexp(v.y)));
+        const double2 v0 = xc0[i];
+        const double2 v1 = two ? xc1[i] : v0;
+        rmax[m] = max(rmax[m], max(max(bexp(v0.x), bexp(v0.y)), max(bexp(v1.x), bexp(v1.y))));
       }
     }
   }
 #pragma unroll
   for (int m = 0; m < MX_ROWS; ++m)
     if (lane + 32 * m < N) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
-  for (int j = warp; j < N; j += nwarp) {
-    const double2* yc = Y + (size_t)j * N;
-    int cm = 0;
+  for (int j = warp; j < N; j += 2 * nwarp) {
+    const int j1 = j + nwarp;
+    const double2* yc0 = Y + (size_t)j * N;
+    const double2* yc1 = Y + (size_t)min(j1, N - 1) * N;
+    int c0 = 0, c1 = 0;
     for (int k = lane; k < N; k += 32) {
-      const double2 v = yc[k];
-      cm = max(cm, max(bexp(v.x), bexp(v.y)));
+      const double2 v0 = yc0[k];
+      const double2 v1 = yc1[k];
+      c0 = max(c0, max(bexp(v0.x), bexp(v0.y)));
+      c1 = max(c1, max(bexp(v1.x), bexp(v1.y)));
     }
-    cm = __reduce_max_sync(0xffffffffu, cm);
-    if (lane == 0) s.expB[j] = cm;
+    c0 = __reduce_max_sync(0xffffffffu, c0);
+    c1 = __reduce_max_sync(0xffffffffu, c1);
+    if (lane == 0) {
+      s.expB[j] = c0;
+      if (j1 < N) s.expB[j1] = c1;
+    }
   }
   __syncthreads();
 }
@@ -519,7 +520,8 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
         const int warp = tid >> 5, lane = tid & 31;
         const int quad = warp & 3, hw = warp >> 2;
         const int row = rb0 + quad * 32 + lane;
-        const int cb = hw * (width / 2), ce = cb + width / 2;
+        // a warp whose 32 tensor-memory lanes are all padding rows has nothing to drain
+        const int cb = hw * (width / 2), ce = rb0 + quad * 32 < N ? cb + width / 2 : cb;
         const int er = row < N ? s.expA[row] : 0;
         const uint32_t bank = (uint32_t)((comp - comp0) * nacc * width);
         for (int c0 = cb; c0 < ce; c0 += 8) {
@@ -555,7 +557,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
                 long long S = 0;
 #pragma unroll
                 for (int a = 0; a < 6; ++a)
-                  if (a < nacc) S += f2ll_int(v[a][jj]);
+                  if (a < nacc) S += __float2ll_rz(__uint_as_float(v[a][jj]) * 0.0078125f);  // / 2^7
                 const double val = assemble(S, er + expB[j] - 1070);
                 const size_t idx = (size_t)row + (size_t)j * N;
                 double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
