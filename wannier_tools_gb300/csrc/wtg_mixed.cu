@@ -32,7 +32,7 @@
 // Operands are staged per K chunk of 16 (one MMA k-step) into a double-buffered
 // shared-memory area in the canonical K-major, no-swizzle layout (8 x 16-byte
 // core matrices; K-adjacent core matrices 128 B apart, 8-row groups 256 B
-// apart).  Warps 1..7 generate a chunk's digit planes while warp 0 issues the
+// apart).  Warps 1..15 generate a chunk's digit planes while warp 0 issues the
 // previous chunk's MMAs (one thread) and commits them to the buffer's mbarrier.
 // Every mbarrier wait is bounded; on a timeout the CTA stops issuing work,
 // marks the instance, waits (bounded) for its MMAs and frees tensor memory.
@@ -46,7 +46,7 @@ namespace {
 
 #include "wtg_fp64_dev.cuh"
 
-constexpr int MX_T = 256;            // threads per CTA (8 warps)
+constexpr int MX_T = 512;            // threads per CTA (16 warps)
 constexpr int NSL = 7;               // digits per operand (49-bit fixed point)
 constexpr int KCH = 16;              // K per staged chunk
 constexpr int APLANE = 128 * KCH * 2;  // bytes of one A plane (128 rows x 16 bf16)
@@ -145,12 +145,10 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7])
-      : "r"(taddr));
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -521,20 +519,21 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
         const int quad = warp & 3, hw = warp >> 2;
         const int row = rb0 + quad * 32 + lane;
         // a warp whose 32 tensor-memory lanes are all padding rows has nothing to drain
-        const int cb = hw * (width / 2), ce = rb0 + quad * 32 < N ? cb + width / 2 : cb;
+        const int nhw = blockDim.x >> 7;
+        const int cb = hw * 4, ce = rb0 + quad * 32 < N ? width : 0;
         const int er = row < N ? s.expA[row] : 0;
         const uint32_t bank = (uint32_t)((comp - comp0) * nacc * width);
-        for (int c0 = cb; c0 < ce; c0 += 8) {
-          uint32_t v[6][8];
+        for (int c0 = cb; c0 < ce; c0 += 4 * nhw) {
+          uint32_t v[6][4];
           const uint32_t ta = st.tmem + bank + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
 #pragma unroll
           for (int a = 0; a < 6; ++a)
-            if (a < nacc) tmem_ld8(ta + (uint32_t)(a * width), v[a]);
+            if (a < nacc) tmem_ld4(ta + (uint32_t)(a * width), v[a]);
           tmem_wait_ld();
           if (row < N) {
-            double old0[8], old1[8];
+            double old0[4], old1[4];
 #pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {            // the epilogue's loads first
+            for (int jj = 0; jj < 4; ++jj) {            // the epilogue's loads first
               const int j = jb + c0 + jj;
               const size_t idx = (size_t)row + (size_t)j * N;
               old0[jj] = 0.0;
@@ -551,7 +550,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
               }
             }
 #pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
+            for (int jj = 0; jj < 4; ++jj) {
               const int j = jb + c0 + jj;
               if (j < N) {
                 long long S = 0;
