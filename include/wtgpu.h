@@ -238,6 +238,29 @@ int wtg_last_error(char* buf, int len);
 int wtg_device_info(char* buf, int len);
 
 /*
+ * Joint density of states along a k path, per omega: the loop of
+ * src/surfstat.f90:889-905 (surfstat's JDOS).  dos(nk, nomega) column-major in
+ * (dos_l, dos_r or their *_only forms), jdos(nk, nomega) out:
+ *   jdos(iq, j) = sum_{ik1} dos(ik1, j) * dos(ik1 + iq - Nh, j),  Nh = (nk-1)/2,
+ * over the reference's ik1 range.  Sums in the reference's order, unfused.
+ */
+int wtg_jdos_kpath(int nk, int nomega, const double* dos, double* jdos);
+
+/*
+ * Quasi-particle interference on a k plane: the JDOS loops of
+ * src/fermiarc.f90:497-545 (SlabQPI_kplane_calc).  chans holds nchan arrays
+ * (nkx, nky) column-major back to back: 1 channel (dos_l_only or dos_r_only)
+ * gives jdos, 4 channels (dos_only, sx, sy, sz) give the spin form jsdos.
+ *   out(q) = scale * sum_{ik2, ik1} sum_c in_c(ik1, ik2) * in_c(k1q, k2q),
+ *   k1q = mod(ik1 + iq1 - 2, p1) + 1, k2q = mod(ik2 + iq2 - 2, p2) + 1,
+ * q = (iq1, iq2) in the reference's ikp order (second index fastest).  The
+ * reference's periods are p1 = nkx-1, p2 = nky-1 for jdos and Nk1-1, Nk2-1 for
+ * jsdos; its jdos is then divided by nkx*nky (scale = 1/(nkx*nky)), jsdos not.
+ */
+int wtg_jdos_kplane(int nkx, int nky, int p1, int p2, int nchan, const double* chans,
+                    double scale, double* jdos);
+
+/*
  * Uneven batches: (k, omega, eta) points of several resident models, of
  * different Ndim, solved in ONE persistent kernel launch.  The CTAs take the
  * points in order of estimated cost (Ndim^3 x an iteration estimate growing as

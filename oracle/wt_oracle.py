@@ -310,6 +310,54 @@ def arc_post(dos_l, dos_r):
     return l_only, r_only
 
 
+def jdos_kpath(dos):
+    """src/surfstat.f90:889-905: along the k path, per omega j and shift
+    iq1 = iq - Nk_half (Nk_half = (knv2-1)/2), the sum over
+    ik1 in [max(-Nk_half-iq1, -Nk_half)+Nk_half+1, min(Nk_half-iq1, Nk_half)+Nk_half+1]
+    of dos(ik1, j)*dos(ik1+iq1, j), accumulated in that order (1-based indices)."""
+    d = np.asarray(dos, dtype=np.float64)
+    nk, nom = d.shape
+    nh = (nk - 1) // 2
+    out = np.zeros((nk, nom))
+    for j in range(nom):
+        col = d[:, j]
+        for iq in range(1, nk + 1):
+            iq1 = iq - nh
+            imin = max(-nh - iq1, -nh) + nh + 1
+            imax = min(nh - iq1, nh) + nh + 1
+            acc = 0.0
+            for ik1 in range(imin, imax + 1):
+                acc = acc + float(col[ik1 - 1]) * float(col[ik1 - 1 + iq1])
+            out[iq - 1, j] = acc
+    return out
+
+
+def qpi_kplane(chans, p1, p2, scale):
+    """src/fermiarc.f90:497-545: for q = (iq1, iq2) in ikp order (i outer,
+    j inner, :140-150), sum over ik2 (outer) and ik1 (inner) of
+    sum_c in_c(ik1, ik2)*in_c(mod(ik1+iq1-2, p1)+1, mod(ik2+iq2-2, p2)+1),
+    the channel products added left to right; times scale (1/(nkx*nky) for
+    jdos, :555-556; 1 for jsdos).  Sequential sums: small grids only."""
+    arrs = [np.asarray(c, dtype=np.float64) for c in chans]
+    nkx, nky = arrs[0].shape
+    out = np.zeros(nkx * nky)
+    q = 0
+    for b1 in range(nkx):
+        for b2 in range(nky):
+            acc = 0.0
+            for a2 in range(nky):
+                c2 = (a2 + b2) % p2
+                for a1 in range(nkx):
+                    c1 = (a1 + b1) % p1
+                    term = float(arrs[0][a1, a2]) * float(arrs[0][c1, c2])
+                    for a in arrs[1:]:
+                        term = term + float(a[a1, a2]) * float(a[c1, c2])
+                    acc = acc + term
+            out[q] = acc if scale == 1.0 else acc * scale
+            q += 1
+    return out
+
+
 def get_hmnr_cell_identity(irvec, ndegen, hmnr, max_ir=8):
     """get_hmnr_cell (src/readHmnR.f90:578-766) for an identity Umatrix with
     every orbital's atom at the same place in both cells, so that

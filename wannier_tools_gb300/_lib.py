@@ -65,6 +65,8 @@ SIGNATURES = {
     "wtg_batch_spectrum": (C.c_int, [C.c_int, C.POINTER(_vp), C.c_int, _ip, _dp, _dp, _dp, C.c_double,
                                       C.c_int, _ip, _ip, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp,
                                       _i32p, _u8p]),
+    "wtg_jdos_kpath": (C.c_int, [C.c_int, C.c_int, _dp, _dp]),
+    "wtg_jdos_kplane": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp]),
     "wtg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "wtg_device_info": (C.c_int, [C.c_char_p, C.c_int]),
 }

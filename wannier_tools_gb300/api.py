@@ -443,6 +443,34 @@ def arc_post(dos_l, dos_r):
             np.where(dos_r < dos_r.max() / 10.0, EPS9, dos_r))
 
 
+def jdos_kpath(dos) -> np.ndarray:
+    """surfstat's joint DOS along the k path (src/surfstat.f90:889-905):
+    dos[nk, nomega] -> jdos[nk, nomega], on the GPU."""
+    d = np.asfortranarray(np.asarray(dos, dtype=np.float64))
+    nk, nom = d.shape
+    out = np.empty((nk, nom), dtype=np.float64, order="F")
+    check(_lib.load().wtg_jdos_kpath(nk, nom, _dptr(d), _dptr(out)))
+    return out
+
+
+def qpi_kplane(chans, p1: int | None = None, p2: int | None = None, scale: float | None = None):
+    """QPI on the k plane (src/fermiarc.f90:497-545) on the GPU.  chans: one
+    (nkx, nky) array (jdos of dos_*_only) or four (dos_only, sx, sy, sz: the
+    spin form).  Periods default to nkx-1, nky-1; scale to 1/(nkx*nky) for one
+    channel and 1 for four, as the reference.  Returns jdos[nkx*nky] in ikp
+    order (second index fastest)."""
+    arrs = [np.asarray(c, dtype=np.float64) for c in (chans if isinstance(chans, (list, tuple)) else [chans])]
+    nkx, nky = arrs[0].shape
+    buf = np.concatenate([np.asfortranarray(a).ravel(order="F") for a in arrs])
+    p1 = nkx - 1 if p1 is None else int(p1)
+    p2 = nky - 1 if p2 is None else int(p2)
+    if scale is None:
+        scale = 1.0 / (nkx * nky) if len(arrs) == 1 else 1.0
+    out = np.empty(nkx * nky, dtype=np.float64)
+    check(_lib.load().wtg_jdos_kplane(nkx, nky, p1, p2, len(arrs), _dptr(buf), float(scale), _dptr(out)))
+    return out
+
+
 def fp64_peak_tflops() -> float:
     """FP64 DFMA throughput of the current GPU (wtg_probe_fp64_peak)."""
     v = C.c_double(0.0)
