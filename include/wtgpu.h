@@ -87,6 +87,25 @@ int wtg_model_create(int nw, int nrpts, const int* irvec, const double* hmnr,
 /* Release a model and all device memory it holds. */
 int wtg_model_destroy(wtg_model_t model);
 
+/*
+ * Phonon models: switch the model's Fourier sum to ham_qlayer2qlayer_LOTO
+ * (src/ham_qlayer2qlayer.f90:312-476, used by SurfaceDOSkk when
+ * LOTO_correction is set, src/fermiarc.f90:215-216): the non-analytic term
+ *   nac(i,j) = kZ(jj,qq) kZ(ii,pp) * 4*3.1415926/(k.D.k * V) * VASPToTHZ/0.529177
+ *              / sqrt(M(ii) M(jj)),   kZ(ii,pp) = k1 Z(ii,1,pp) + k2 Z(ii,2,pp),
+ * is added to every H(R) before the sum, and k is moved to (1e-4, 1e-4) when
+ * |k|^2 <= 1e-4 (all with the reference's constants).  Applies to
+ * wtg_ham_qlayer2qlayer and the spectrum entry points of this model.
+ *   born[natoms*3*3]  Born_Charge(natoms, 3, 3), column-major
+ *   diele[9]          Diele_Tensor(3, 3), column-major
+ *   masses[natoms]    Atom_Mass;  cell_volume  Origin_cell%CellVolume
+ * Num_wann must be 3*natoms.  natoms = 0 switches the correction off.
+ * (The overlap variant s_qlayer2qlayer, src/ham_qlayer2qlayer.f90:104-205, is
+ * wtg_ham_qlayer2qlayer of a model created from SmnR instead of HmnR.)
+ */
+int wtg_model_set_loto(wtg_model_t model, int natoms, const double* born, const double* diele,
+                       const double* masses, double cell_volume);
+
 /* Ndim = nw*np of a model (or < 0 on a bad handle). */
 int wtg_model_ndim(wtg_model_t model);
 

@@ -85,6 +85,41 @@ def ham_qlayer2qlayer(k, hmnr, irvec, ndegen, nw, np_, ijmax=IJMAX_REF):
     return h00, h01
 
 
+VASP_TO_THZ = 29.54263748                    # src/module.f90:1042
+
+
+def ham_qlayer2qlayer_loto(k, hmnr, irvec, ndegen, nw, np_, born, diele, masses, cell_volume,
+                           ijmax=IJMAX_REF):
+    """ham_qlayer2qlayer_LOTO (src/ham_qlayer2qlayer.f90:312-476) for an identity
+    lattice transform: k moved to (1e-4, 1e-4) when |k|^2 <= 1e-4 (:366-370);
+    temp1(qq) = k1 D(qq,1) + k2 D(qq,2), temp2 = k.temp1 (:372-375);
+    constant_t = 4*3.1415926/(temp2*V)*VASPToTHZ/0.529177 (:376, the literal
+    3.1415926 kept); kBorn(ii,pp) = k1 Z(ii,1,pp) + k2 Z(ii,2,pp) (:378-382);
+    nac(i,j) = kBorn(jj,qq) kBorn(ii,pp) constant_t / sqrt(M(ii) M(jj)) added to
+    HmnR(:,:,iR) before the phase sum (:395-406).  born (natoms, 3, 3),
+    diele (3, 3), masses (natoms,)."""
+    kn = [float(k[0]), float(k[1])]
+    if abs(kn[0] ** 2 + kn[1] ** 2) <= 0.0001:
+        kn = [0.0001, 0.0001]
+    z = np.asarray(born, dtype=np.float64)
+    d = np.asarray(diele, dtype=np.float64)
+    mass = np.asarray(masses, dtype=np.float64)
+    natoms = z.shape[0]
+    temp1 = [kn[0] * d[q, 0] + kn[1] * d[q, 1] for q in range(2)]
+    temp2 = kn[0] * temp1[0] + kn[1] * temp1[1]
+    constant_t = 4.0 * 3.1415926 / (temp2 * cell_volume) * VASP_TO_THZ / 0.529177
+    kborn = np.array([[kn[0] * z[ii, 0, pp] + kn[1] * z[ii, 1, pp] for pp in range(3)]
+                      for ii in range(natoms)])
+    nac = np.zeros((nw, nw))
+    for ii in range(natoms):
+        for pp in range(3):
+            for jj in range(natoms):
+                for qq in range(3):
+                    nac[ii * 3 + pp, jj * 3 + qq] = (kborn[jj, qq] * kborn[ii, pp] * constant_t
+                                                     / math.sqrt(mass[ii] * mass[jj]))
+    return ham_qlayer2qlayer(kn, np.asarray(hmnr) + nac[None, :, :], irvec, ndegen, nw, np_, ijmax)
+
+
 def inv(a):
     """src/inverse.f90:1-58: zgesv with an identity right-hand side.
 
@@ -259,7 +294,7 @@ def kplane_grid(nk1, nk2, k2d_start, vec1, vec2):
 
 def surface_spectrum(hmnr, irvec, ndegen, nw, np_, kpts, omegas, eta, top, bot,
                      scale=1.0, accuracy=ACCURACY_REF, itermax=ITERMAX_REF,
-                     ijmax=IJMAX_REF, with_spin=False):
+                     ijmax=IJMAX_REF, with_spin=False, loto=None):
     """Loop body of surfstat (src/surfstat.f90:123-197) / SurfaceDOSkk
     (src/fermiarc.f90:206-248) over an explicit (k, omega) list.
 
@@ -274,7 +309,10 @@ def surface_spectrum(hmnr, irvec, ndegen, nw, np_, kpts, omegas, eta, top, bot,
         for name in ("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r"):
             out[name] = np.zeros((nk, nwo))
     for ik in range(nk):
-        h00, h01 = ham_qlayer2qlayer(kpts[ik], hmnr, irvec, ndegen, nw, np_, ijmax)
+        if loto is None:
+            h00, h01 = ham_qlayer2qlayer(kpts[ik], hmnr, irvec, ndegen, nw, np_, ijmax)
+        else:
+            h00, h01 = ham_qlayer2qlayer_loto(kpts[ik], hmnr, irvec, ndegen, nw, np_, *loto, ijmax=ijmax)
         for j in range(nwo):
             gll, grr, gb, it, st = surfgreen_1985(omegas[j], h00, h01, eta, accuracy, itermax)
             dl, dr, db = spectral_sums(gll, grr, gb, top, bot, nw, scale)

@@ -36,6 +36,7 @@ SIGNATURES = {
     "wtg_model_create": (C.c_int, [C.c_int, C.c_int, _ip, _dp, _ip, C.c_int, C.c_int, C.POINTER(_vp)]),
     "wtg_model_destroy": (C.c_int, [_vp]),
     "wtg_model_ndim": (C.c_int, [_vp]),
+    "wtg_model_set_loto": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.c_double]),
     "wtg_ham_qlayer2qlayer": (C.c_int, [_vp, _dp, _dp, _dp]),
     "wtg_surfgreen_1985": (C.c_int, [C.c_int, C.c_double, C.c_double, _dp, _dp, C.c_double, C.c_int,
                                       _dp, _dp, _dp, _ip, _ip]),

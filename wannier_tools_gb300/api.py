@@ -97,6 +97,23 @@ class Model:
     def __exit__(self, *exc):
         self.close()
 
+    def set_loto(self, born, diele=None, masses=None, cell_volume: float = 0.0):
+        """Phonon LO-TO correction (ham_qlayer2qlayer_LOTO,
+        src/ham_qlayer2qlayer.f90:312-476) for this model's Fourier sums.
+        born: Born_Charge (natoms, 3, 3); diele: Diele_Tensor (3, 3); masses:
+        Atom_Mass (natoms); cell_volume in the reference's units.  born=None
+        switches it off."""
+        lib = _lib.load()
+        if born is None:
+            check(lib.wtg_model_set_loto(self._handle, 0, None, None, None, 0.0))
+            return
+        z = np.asfortranarray(np.asarray(born, dtype=np.float64))
+        d = np.asfortranarray(np.asarray(diele, dtype=np.float64))
+        mm = np.ascontiguousarray(masses, dtype=np.float64)
+        self._loto = (z, d, mm)
+        check(lib.wtg_model_set_loto(self._handle, int(z.shape[0]), _dptr(z.ravel(order="F")),
+                                     _dptr(d.ravel(order="F")), _dptr(mm), float(cell_volume)))
+
     # -- ham_qlayer2qlayer -------------------------------------------------
     def ham_qlayer2qlayer(self, k) -> tuple[np.ndarray, np.ndarray]:
         kk = np.ascontiguousarray(np.asarray(k, dtype=np.float64).reshape(2))
@@ -400,10 +417,13 @@ def kplane_slab(nk1: int, nk2: int, k2d_start, vec1, vec2):
 
 
 def surfstat(model: Model, k2_path, omegamin: float, omegamax: float, omeganum: int, top, bot,
-             tol: float = ACCURACY_REF, itermax: int = ITERMAX_REF) -> dict:
+             tol: float = ACCURACY_REF, itermax: int = ITERMAX_REF, particle: str = "electron") -> dict:
     """surfstat (src/surfstat.f90:1-260) without file output: returns raw
-    sums plus the written quantities log|dos| and *_only."""
+    sums plus the written quantities log|dos| and *_only.  For phonons the
+    omega grid is squared after eta is set (src/surfstat.f90:90-96)."""
     omega, eta = surfstat_grid(omegamin, omegamax, omeganum)
+    if "phonon" in particle:
+        omega = omega * omega
     r = model.surface_spectrum(k2_path, omega, eta, top, bot, tol, itermax, divide_by_pi=False)
     r["omega"] = omega
     r["eta"] = eta
@@ -413,9 +433,13 @@ def surfstat(model: Model, k2_path, omegamin: float, omegamax: float, omeganum: 
 
 def surface_dos_kk(model: Model, nk1: int, nk2: int, k2d_start, vec1, vec2, iso_energy: float,
                    fermi_broadening: float, top, bot, tol: float = ACCURACY_REF,
-                   itermax: int = ITERMAX_REF) -> dict:
-    """SurfaceDOSkk arc maps (src/fermiarc.f90:1-460) without file output."""
+                   itermax: int = ITERMAX_REF, particle: str = "electron") -> dict:
+    """SurfaceDOSkk arc maps (src/fermiarc.f90:1-460) without file output.
+    For phonons the energy is squared (src/fermiarc.f90:196-200); the LO-TO
+    form follows Model.set_loto."""
     nkx, nky, k12 = kplane_slab(nk1, nk2, k2d_start, vec1, vec2)
+    if "phonon" in particle:
+        iso_energy = iso_energy * iso_energy
     r = model.surface_spectrum(k12, [iso_energy], fermi_broadening, top, bot, tol, itermax,
                                divide_by_pi=True)
     out = {name: r[name][:, 0].reshape(nkx, nky) for name in ("dos_l", "dos_r", "dos_bulk", "iters", "status")}

@@ -73,6 +73,12 @@ struct wtg_model {
   double2* d_hr = nullptr;
   double2* d_rab = nullptr;
   int* d_icoff = nullptr;
+  double* d_wr = nullptr;              // 1 / ndegen of the used R vectors
+  // phonon LO-TO correction (wtg_model_set_loto)
+  int loto = 0;
+  DevBuf d_lz, d_lm;
+  double ld[4] = {0, 0, 0, 0};
+  double lvol = 0.0;
   DevBuf phase, h, ws, counter;
   // staging for the host-pointer entry points
   DevBuf k_in, w_in, out_dos, out_it, out_st;
@@ -96,6 +102,15 @@ struct wtg_model {
 };
 
 namespace {
+
+void set_loto_args(const wtg_model* m, wtg::FourierArgs& f) {
+  f.loto = m->loto;
+  f.wr = m->d_wr;
+  f.lz = (const double*)m->d_lz.p;
+  f.lmass = (const double*)m->d_lm.p;
+  for (int i = 0; i < 4; ++i) f.ld[i] = m->ld[i];
+  f.lvol = m->lvol;
+}
 
 int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const double* d_omega,
                  double eta, double tol, int itermax, int ntop, const int* top, int nbot,
@@ -170,6 +185,7 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
     f.k0 = k0;
     f.kc = kc;
     f.rab = m->d_rab;
+    set_loto_args(m, f);
     f.hr = m->d_hr;
     f.icoff = m->d_icoff;
     f.ic_lo = m->ic_lo;
@@ -291,6 +307,8 @@ int engine_create(int nmodels, const wtg_model_t* models, int precision, int max
   int max_n = 0, max_nru = 1, dev = -1;
   for (int i = 0; i < nmodels; ++i) {
     if (!models[i]) return fail(WTG_EINVAL, "null model");
+    if (models[i]->loto)
+      return fail(WTG_EUNSUPPORTED, "batch engines take models without the LO-TO correction");
     if (dev >= 0 && models[i]->device != dev) return fail(WTG_EINVAL, "models on different devices");
     dev = models[i]->device;
     max_n = std::max(max_n, models[i]->N);
@@ -517,9 +535,11 @@ int wtg_model_create(int nw, int nrpts, const int* irvec, const double* hmnr, co
   const size_t nw2 = (size_t)nw * nw;
   std::vector<double2> hr(std::max<size_t>(1, nw2 * m->nRu));
   std::vector<double2> rab(std::max(1, m->nRu));
+  std::vector<double> wr(std::max(1, m->nRu));
   for (int u = 0; u < m->nRu; ++u) {
     const int r = order[u];
     const double nd = ndegen ? (double)ndegen[r] : 1.0;
+    wr[u] = 1.0 / nd;
     if (nd == 0.0) {
       delete m;
       return fail(WTG_EINVAL, "ndegen entry is zero");
@@ -534,6 +554,8 @@ int wtg_model_create(int nw, int nrpts, const int* irvec, const double* hmnr, co
   if (e == cudaSuccess) e = cudaMalloc(&m->d_hr, sizeof(double2) * hr.size());
   if (e == cudaSuccess) e = cudaMalloc(&m->d_rab, sizeof(double2) * rab.size());
   if (e == cudaSuccess) e = cudaMalloc(&m->d_icoff, sizeof(int) * icoff.size());
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_wr, sizeof(double) * wr.size());
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_wr, wr.data(), sizeof(double) * wr.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->d_hr, hr.data(), sizeof(double2) * hr.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->d_rab, rab.data(), sizeof(double2) * rab.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->d_icoff, icoff.data(), sizeof(int) * icoff.size(), cudaMemcpyHostToDevice);
@@ -548,6 +570,39 @@ int wtg_model_create(int nw, int nrpts, const int* irvec, const double* hmnr, co
   return WTG_OK;
 }
 
+int wtg_model_set_loto(wtg_model_t m, int natoms, const double* born, const double* diele,
+                       const double* masses, double cell_volume) {
+  if (!m) return fail(WTG_EINVAL, "null model");
+  std::lock_guard<std::mutex> lk(m->mu);
+  if (natoms == 0) {
+    m->loto = 0;
+    return WTG_OK;
+  }
+  if (natoms < 0 || !born || !diele || !masses) return fail(WTG_EINVAL, "bad argument");
+  if (3 * natoms != m->nw) return fail(WTG_EINVAL, "Num_wann must be 3 x natoms for phonons");
+  for (int i = 0; i < natoms; ++i)
+    if (!(masses[i] > 0.0)) return fail(WTG_EINVAL, "masses must be > 0");
+  WTG_CK(cudaSetDevice(m->device));
+  // Born_Charge(atom, k direction 1..2, cartesian 1..3) from the Fortran (natoms, 3, 3) array
+  std::vector<double> lz((size_t)natoms * 6);
+  for (int i = 0; i < natoms; ++i)
+    for (int a = 0; a < 2; ++a)
+      for (int p = 0; p < 3; ++p) lz[(i * 2 + a) * 3 + p] = born[i + natoms * (a + 3 * p)];
+  WTG_CK(cudaEventSynchronize(m->done));
+  WTG_CK(m->d_lz.ensure(sizeof(double) * lz.size()));
+  WTG_CK(m->d_lm.ensure(sizeof(double) * natoms));
+  WTG_CK(cudaMemcpy(m->d_lz.p, lz.data(), sizeof(double) * lz.size(), cudaMemcpyHostToDevice));
+  WTG_CK(cudaMemcpy(m->d_lm.p, masses, sizeof(double) * natoms, cudaMemcpyHostToDevice));
+  // Diele_Tensor(qq, 1..2) for qq = 1, 2 from the Fortran (3, 3) array
+  m->ld[0] = diele[0];
+  m->ld[1] = diele[3];
+  m->ld[2] = diele[1];
+  m->ld[3] = diele[4];
+  m->lvol = cell_volume;
+  m->loto = 1;
+  return WTG_OK;
+}
+
 int wtg_model_destroy(wtg_model_t m) {
   if (!m) return fail(WTG_EINVAL, "null model");
   {
@@ -557,6 +612,9 @@ int wtg_model_destroy(wtg_model_t m) {
     cudaFree(m->d_hr);
     cudaFree(m->d_rab);
     cudaFree(m->d_icoff);
+    cudaFree(m->d_wr);
+    m->d_lz.release();
+    m->d_lm.release();
     m->phase.release();
     m->h.release();
     m->ws.release();
@@ -596,6 +654,7 @@ int wtg_ham_qlayer2qlayer(wtg_model_t m, const double* k, double* h00, double* h
   f.k0 = 0;
   f.kc = 1;
   f.rab = m->d_rab;
+  set_loto_args(m, f);
   f.hr = m->d_hr;
   f.icoff = m->d_icoff;
   f.ic_lo = m->ic_lo;

@@ -84,6 +84,13 @@ struct FourierArgs {
   int nRu, nw, np, ijmax;
   double2* phase;         // [kc][nRu] scratch
   double2* h;             // [kc][2][N*N] output: H00 then H01, column-major
+  // phonon LO-TO correction (ham_qlayer2qlayer_LOTO); loto = 0: plain sum
+  int loto;
+  const double* wr;       // [nRu] 1 / ndegen of the used R vectors
+  const double* lz;       // [natoms][2][3] Born charges Z(atom, k direction, cartesian)
+  const double* lmass;    // [natoms] atomic masses
+  double ld[4];           // in-plane dielectric tensor D(1,1), D(1,2), D(2,1), D(2,2)
+  double lvol;            // cell volume
 };
 void launch_fourier(const FourierArgs& a, cudaStream_t s);
 

@@ -15,12 +15,23 @@ namespace wtg {
 constexpr int FK = 8;          // k points per thread
 constexpr int FT = 128;        // threads per CTA
 
+// the LO-TO form evaluates everything at k shifted off Gamma:
+// |k|^2 <= 1e-4 -> k = (1e-4, 1e-4) (src/ham_qlayer2qlayer.f90:366-370)
+__device__ __forceinline__ void loto_k(double& k1, double& k2) {
+  if (fabs(k1 * k1 + k2 * k2) <= 0.0001) {
+    k1 = 0.0001;
+    k2 = 0.0001;
+  }
+}
+
 __global__ void k_phases(const double* __restrict__ k, int nk_total, int k0, int kc,
-                         const double2* __restrict__ rab, int nRu, double2* __restrict__ phase) {
+                         const double2* __restrict__ rab, int nRu, double2* __restrict__ phase,
+                         int loto) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)kc * nRu) return;
   const int ikl = (int)(t / nRu), r = (int)(t % nRu);
-  const double k1 = k[k0 + ikl], k2 = k[k0 + ikl + nk_total];
+  double k1 = k[k0 + ikl], k2 = k[k0 + ikl + nk_total];
+  if (loto) loto_k(k1, k2);
   const double kdotr = k1 * rab[r].x + k2 * rab[r].y;      // src/ham_qlayer2qlayer.f90:55
   double s, c;
   sincos(2.0 * PI_REF * kdotr, &s, &c);                     // :56
@@ -45,6 +56,33 @@ __global__ void __launch_bounds__(FT) k_fourier(const FourierArgs a) {
       if (kb + f < a.kc) cfma(acc[f], hv, __ldg(a.phase + (size_t)(kb + f) * a.nRu + r));
     }
   }
+  if (a.loto) {
+    // src/ham_qlayer2qlayer.f90:372-413: the k-dependent non-analytic term
+    // nac(i, j) = kZ(j) kZ(i) c / sqrt(M(ii) M(jj)) is added to every H(R) of
+    // the group, i.e. nac times the group's sum of phase / ndegen
+    const int ie = e % a.nw, je = e / a.nw;
+    const int ii = ie / 3, pp = ie % 3, jj = je / 3, qq = je % 3;
+    for (int f = 0; f < FK; ++f) {
+      if (kb + f >= a.kc) break;
+      double k1 = a.k[a.k0 + kb + f], k2 = a.k[a.k0 + kb + f + a.nk_total];
+      loto_k(k1, k2);
+      const double t1 = k1 * a.ld[0] + k2 * a.ld[1], t2 = k1 * a.ld[2] + k2 * a.ld[3];
+      const double temp2 = k1 * t1 + k2 * t2;
+      const double c = 4.0 * 3.1415926 / (temp2 * a.lvol) * 29.54263748 / 0.529177;
+      const double kzi = k1 * a.lz[(ii * 2 + 0) * 3 + pp] + k2 * a.lz[(ii * 2 + 1) * 3 + pp];
+      const double kzj = k1 * a.lz[(jj * 2 + 0) * 3 + qq] + k2 * a.lz[(jj * 2 + 1) * 3 + qq];
+      const double nac = kzj * kzi * c / sqrt(a.lmass[ii] * a.lmass[jj]);
+      double2 ps = make_double2(0.0, 0.0);
+      for (int r = a.icoff[g]; r < r1; ++r) {
+        const double2 ph = __ldg(a.phase + (size_t)(kb + f) * a.nRu + r);
+        const double w = __ldg(a.wr + r);
+        ps.x = fma(ph.x, w, ps.x);
+        ps.y = fma(ph.y, w, ps.y);
+      }
+      acc[f].x = fma(nac, ps.x, acc[f].x);
+      acc[f].y = fma(nac, ps.y, acc[f].y);
+    }
+  }
   const int N = a.nw * a.np;
   const int ie = e % a.nw, je = e / a.nw;
   for (int f = 0; f < FK; ++f) {
@@ -64,7 +102,7 @@ void launch_fourier(const FourierArgs& a, cudaStream_t s) {
   const long nph = (long)a.kc * a.nRu;
   if (nph > 0) {
     k_phases<<<(unsigned)((nph + 255) / 256), 256, 0, s>>>(a.k, a.nk_total, a.k0, a.kc, a.rab,
-                                                          a.nRu, a.phase);
+                                                          a.nRu, a.phase, a.loto);
   }
   const int N = a.nw * a.np;
   cudaMemsetAsync(a.h, 0, sizeof(double2) * (size_t)a.kc * 2 * N * N, s);
