@@ -17,11 +17,12 @@
 //   * the accumulators are read back (tcgen05.ld), converted to integers and
 //     summed in int64, and the FP64 result is assembled with integer
 //     operations (no FP64 arithmetic for the product itself).
-// The complex product runs in passes over row blocks of 128 (the MMA's M):
-// Cr = Xr Yr - Xi Yi (the second term via the instruction's negate-B bit) and
-// Ci = Xr Yi + Xi Yr, both in one pass when their accumulators fit the 512
-// tensor-memory columns (Ndim <= 48), else one component per pass over as many
-// column blocks as the accumulators need (MxPlan).
+// The complex product runs in passes over row blocks of 128 (the MMA's M) and
+// column blocks of w <= 48 (40 above Ndim 256): the B digit planes are stored
+// as -Yi, Yr, Yi, so that per slice pair two MMAs of N = 2w, Xr [Yr; Yi] and
+// Xi [-Yi; Yr], accumulate [Cr | Ci] = [Xr Yr - Xi Yi | Xr Yi + Xi Yr]; both
+// components share one generation of the A planes and every MMA is twice as
+// wide (MxPlan).
 // Inverses (zgesv with identity, src/inverse.f90:43-55) are an FP32
 // Gauss-Jordan (shared memory up to Ndim 112, global memory in panels above)
 // followed by Newton-Schulz refinement X <- X + X (I - M X) whose two products
@@ -60,12 +61,12 @@ constexpr int MX_PANEL = 16;         // pivot steps per panel of the global-memo
 constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident column
 
 // How one product is cut into tensor-memory passes.  Rows go in blocks of
-// M = 128.  Each pass holds nacc FP32 accumulators of w columns for one
-// component (or both components when they fit: both = 1), so 512 tensor-memory
-// columns bound nacc * w; output columns [0, NP) go in ncb blocks of w0 (the
-// last block narrower).  nacc = 5 keeps slice orders 2..5 exact for K <= 256;
-// above that order 5 is split over two K halves (nacc = 6), since 4 * 127^2 * K
-// must stay below 2^24.
+// M = 128.  Each pass holds nacc FP32 accumulators of 2w columns (both
+// components side by side), so 512 tensor-memory columns bound 2 nacc w;
+// output columns [0, NP) go in ncb blocks of w0 (a multiple of 8; the last
+// block narrower).  nacc = 5 keeps slice orders 2..5 exact for K <= 256; above
+// that order 5 is split over two K halves (nacc = 6), since 4 * 127^2 * K must
+// stay below 2^24.
 struct MxPlan {
   int N, NP, nrb, nacc, both, ncb, w0;
   int wb;                    // B-plane width of the shared-memory layout (>= w0)
@@ -77,18 +78,12 @@ __host__ __device__ inline MxPlan mx_plan(int N) {
   p.NP = (N + 15) & ~15;
   p.nrb = (N + 127) / 128;
   p.nacc = N > 256 ? 6 : 5;
-  p.both = 2 * p.nacc * p.NP <= 512 ? 1 : 0;
-  if (p.both) {
-    p.ncb = 1;
-    p.w0 = p.NP;
-  } else {
-    p.ncb = (p.nacc * p.NP + 511) / 512;
-    for (;;) {
-      p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 15) & ~15;
-      if (p.nacc * p.w0 <= 512) break;
-      ++p.ncb;
-    }
-  }
+  // both components side by side in one pass: 2 x nacc accumulators of w columns
+  const int wmax = (512 / (2 * p.nacc)) & ~7;
+  p.ncb = (p.NP + wmax - 1) / wmax;
+  p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 7) & ~7;
+  while (p.ncb > 1 && (p.ncb - 1) * p.w0 >= p.NP) --p.ncb;
+  p.both = 1;
   p.wb = p.w0;
   return p;
 }
@@ -228,7 +223,7 @@ struct MxShared {
 };
 
 __host__ __device__ __forceinline__ int bufbytes_of(int WB) {
-  return 2 * NSL * APLANE + 2 * NSL * WB * KCH * 2;
+  return 2 * NSL * APLANE + 3 * NSL * WB * KCH * 2;
 }
 
 // shared-memory layout: two operand buffers (the FP32 Gauss-Jordan matrix
@@ -364,12 +359,29 @@ __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned 
 #undef WTG_PUT
 }
 
-// digit planes of chunk [k0, k0+16) into buffer b: A = rows [rb0, rb0+128) of
-// X, B = columns [jb, jb+width) of Y (as rows of the K-major B^T layout).
-// Work item `it` covers rows (or columns) 8 (it >> 6) + (lane >> 2) and K pair
-// 8 ((it >> 5) & 1) + 2 (lane & 3); in the canonical layout its word sits at
-// byte 4 it of a plane, so each warp store fills one 128-byte core matrix
-// (no bank conflicts).  Generated by threads gtid = 0 .. gthreads-1.
+// the B digit planes of one element pair: per digit q the planes -Yi, Yr, Yi
+// (3(q-1), +1, +2), so that [Yr; Yi] and [-Yi; Yr] are each one operand of 2w
+// rows; -Yi is Yi with both BF16 sign bits flipped
+__device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigned long long fr0,
+                                             unsigned long long fr1, unsigned long long fi0,
+                                             unsigned long long fi1, uint32_t sr, uint32_t si) {
+  const uint32_t hr0 = (uint32_t)(fr0 >> 21), lr0 = (uint32_t)fr0 & 0x1FFFFFu;
+  const uint32_t hr1 = (uint32_t)(fr1 >> 21), lr1 = (uint32_t)fr1 & 0x1FFFFFu;
+  const uint32_t hi0 = (uint32_t)(fi0 >> 21), li0 = (uint32_t)fi0 & 0x1FFFFFu;
+  const uint32_t hi1 = (uint32_t)(fi1 >> 21), li1 = (uint32_t)fi1 & 0x1FFFFFu;
+#define WTG_PUTB(P)                                                                         \
+  {                                                                                          \
+    constexpr float sc = pow2f(7 * (5 - P)), off = -pow2f(23 + 7 * (5 - P));               \
+    const uint32_t br = dig2f(digit7<P>(hr0, lr0), digit7<P>(hr1, lr1), sc, off, sr);       \
+    const uint32_t bi = dig2f(digit7<P>(hi0, li0), digit7<P>(hi1, li1), sc, off, si);       \
+    dst[(3 * (P - 1)) * pstride] = bi ^ 0x80008000u;                                         \
+    dst[(3 * (P - 1) + 1) * pstride] = br;                                                   \
+    dst[(3 * (P - 1) + 2) * pstride] = bi;                                                   \
+  }
+  WTG_PUTB(1) WTG_PUTB(2) WTG_PUTB(3) WTG_PUTB(4) WTG_PUTB(5) WTG_PUTB(6) WTG_PUTB(7)
+#undef WTG_PUTB
+}
+
 // digit planes of chunk [k0, k0+16) into buffer b: A = rows [rb0, rb0+128) of
 // X, B = columns [jb, jb+width) of Y (as rows of the K-major B^T layout).
 // Work item `it` covers rows (or columns) 8 (it >> 6) + (lane >> 2) and K pair
@@ -383,7 +395,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
   unsigned char* __restrict__ B = A + 2 * NSL * APLANE;
   const int* __restrict__ expA = s.expA;
   const int* __restrict__ expB = s.expB;
-  const int bstride = WB * KCH * 2 / 4;           // B plane stride in words
+  const int bstride = width * KCH * 2 / 4;        // B plane stride in words (= pass width)
   for (int it = gtid; it < 128 * (KCH / 2); it += gthreads) {
     const int cm = it >> 5, ln = it & 31;
     const int il = (cm >> 1) * 8 + (ln >> 2), kk = (cm & 1) * 8 + (ln & 3) * 2, i = rb0 + il;
@@ -409,7 +421,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     uint32_t* dst = reinterpret_cast<uint32_t*>(B) + it;
     if (j >= N) {                                  // padding columns
 #pragma unroll
-      for (int pl = 0; pl < 2 * NSL; ++pl) dst[pl * bstride] = 0u;
+      for (int pl = 0; pl < 3 * NSL; ++pl) dst[pl * bstride] = 0u;
       continue;
     }
     const int F = expB[j];
@@ -419,25 +431,26 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(y0.x, F, n0r), f0i = fixed49(y0.y, F, n0i);
     const unsigned long long f1r = fixed49(y1.x, F, n1r), f1i = fixed49(y1.y, F, n1i);
-    put_digits<5>(dst, bstride, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
-                  (n0i << 15) | (n1i << 31));
+    put_digits_b(dst, bstride, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
+                 (n0i << 15) | (n1i << 31));
   }
 }
 
 // all slice-pair MMAs of one chunk (thread 0 only).  The descriptors' start
 // address field holds (address >> 4) in its low 14 bits, so a plane offset is
-// added to a base descriptor directly.  Slice order t = p + q goes to
-// accumulator t - 2 for t <= 5 (with nacc = 6, order 5 of the second K half to
-// accumulator 4) and to the last accumulator for t >= 6; accumulator a sits at
-// tensor-memory column bank + a * width.  amask holds the accumulators already
-// written in this pass (bit abase + a): the first MMA into one overwrites.
-__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int WB, int width, int comp,
-                         uint32_t bank, int nacc, int khalf, uint32_t& amask, int abase) {
+// added to a base descriptor directly.  Both components in two MMAs of N = 2w
+// per slice pair: Xr [Yr; Yi] and Xi [-Yi; Yr] accumulate [Cr | Ci].  Slice
+// order t = p + q goes to accumulator t - 2 for t <= 5 (with nacc = 6, order 5
+// of the second K half to accumulator 4) and to the last accumulator for
+// t >= 6; accumulator a sits at tensor-memory column 2 w a.  amask holds the
+// accumulators already written in this pass: the first MMA into one overwrites.
+__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int nacc, int khalf,
+                         uint32_t& amask) {
   const uint32_t A = saddr(s.buf[b]);
   const uint32_t B = A + 2 * NSL * APLANE;
-  const uint64_t bplane16 = (uint64_t)WB * KCH * 2 >> 4;
+  const uint64_t bplane16 = (uint64_t)width * KCH * 2 >> 4;
   const uint64_t adesc0 = sdesc(A), bdesc0 = sdesc(B);
-  const uint32_t id_pos = idesc(width, 0), id_neg = idesc(width, 1);
+  const uint32_t id2 = idesc(2 * width, 0);
 #pragma unroll 1
   for (int p = 1; p <= NSL; ++p) {
     const uint64_t aR = adesc0 + (uint64_t)(2 * (p - 1)) * (APLANE >> 4);
@@ -446,19 +459,14 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int WB, int wi
     for (int q = 1; q + p <= NSL + 1; ++q) {
       const int t = p + q;
       const int a = t <= 4 ? t - 2 : (t == 5 ? 3 + khalf : nacc - 1);
-      const uint32_t d = tmem + bank + (uint32_t)(a * width);
-      const uint64_t bR = bdesc0 + (uint64_t)(2 * (q - 1)) * bplane16;
-      const uint64_t bI = bR + bplane16;
-      const uint32_t bit = 1u << (abase + a);
+      const uint32_t d = tmem + (uint32_t)(a * 2 * width);
+      const uint64_t bNR = bdesc0 + (uint64_t)(3 * (q - 1)) * bplane16;   // [-Yi; Yr]
+      const uint64_t bRI = bNR + bplane16;                                 // [Yr; Yi]
+      const uint32_t bit = 1u << a;
       const uint32_t acc = (amask & bit) ? 1u : 0u;
       amask |= bit;
-      if (comp == 0) {          // Cr = Xr Yr - Xi Yi
-        mma_bf16(d, aR, bR, id_pos, acc);
-        mma_bf16(d, aI, bI, id_neg, 1u);
-      } else {                  // Ci = Xr Yi + Xi Yr
-        mma_bf16(d, aR, bI, id_pos, acc);
-        mma_bf16(d, aI, bR, id_pos, 1u);
-      }
+      mma_bf16(d, aR, bRI, id2, acc);
+      mma_bf16(d, aI, bNR, id2, 1u);
     }
   }
 }
@@ -472,15 +480,15 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
   const int N = pl.N, tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
   const int nacc = pl.nacc, WB = pl.wb;
-  const int npass = pl.both ? 1 : 2 * pl.ncb;
+  const int npass = pl.ncb;
   float nrm = 0.f;
   oz_exponents(X, Y, N, s);
   __syncthreads();
   for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
     const int rb0 = rb * 128;
     for (int pass = 0; pass < npass && !st.abort; ++pass) {
-      const int comp0 = pl.both ? 0 : pass / pl.ncb, comp1 = pl.both ? 1 : comp0;
-      const int cbi = pl.both ? 0 : pass % pl.ncb;
+      const int comp0 = 0, comp1 = 1;
+      const int cbi = pass;
       const int jb = cbi * pl.w0;
       const int width = min(pl.w0, pl.NP - jb);
       uint32_t amask = 0u;
@@ -497,9 +505,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
         if (st.abort) break;
         if (tid == 0) {
           const int khalf = (nacc == 6 && 2 * c >= nch) ? 1 : 0;
-          for (int comp = comp0; comp <= comp1; ++comp)
-            oz_issue(s, st.tmem, b, WB, width, comp, (uint32_t)((comp - comp0) * nacc * width),
-                     nacc, khalf, amask, 8 * (comp - comp0));
+          oz_issue(s, st.tmem, b, width, nacc, khalf, amask);
           mma_commit(&s.mbar[b]);
         }
         st.ncommit[b] += 1;
@@ -522,13 +528,13 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
         const int nhw = blockDim.x >> 7;
         const int cb = hw * 4, ce = rb0 + quad * 32 < N ? width : 0;
         const int er = row < N ? s.expA[row] : 0;
-        const uint32_t bank = (uint32_t)((comp - comp0) * nacc * width);
+        const uint32_t bank = (uint32_t)(comp * width);
         for (int c0 = cb; c0 < ce; c0 += 4 * nhw) {
           uint32_t v[6][4];
           const uint32_t ta = st.tmem + bank + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
 #pragma unroll
           for (int a = 0; a < 6; ++a)
-            if (a < nacc) tmem_ld4(ta + (uint32_t)(a * width), v[a]);
+            if (a < nacc) tmem_ld4(ta + (uint32_t)(a * 2 * width), v[a]);
           tmem_wait_ld();
           if (row < N) {
             double old0[4], old1[4];
