@@ -167,6 +167,16 @@ __device__ __forceinline__ unsigned long long fixed49(double x, int E, unsigned&
   return sh < 64 ? (m >> sh) : 0ull;
 }
 
+// integer value of an integer-valued float, divided by 2^7 (truncating)
+__device__ __forceinline__ long long f2ll_bits(uint32_t w) {
+  const int e = (int)((w >> 23) & 0xFF);
+  if (e < 134) return 0;
+  const long long m = (long long)((w & 0x7FFFFFu) | 0x800000u);
+  const int sh = e - 157;
+  const long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
+  return (w >> 31) ? -v : v;
+}
+
 // double with value S * 2^(be0 - 1023) assembled from bits (truncating)
 __device__ __forceinline__ double assemble(long long S, int be0) {
   if (S == 0) return 0.0;
@@ -561,8 +571,17 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
               if (j < N) {
                 long long S = 0;
 #pragma unroll
-                for (int a = 0; a < 6; ++a)
-                  if (a < nacc) S += __float2ll_rz(__uint_as_float(v[a][jj]) * 0.0078125f);  // / 2^7
+                for (int a = 0; a < 6; ++a) {
+                  if (a >= nacc) continue;
+                  if (a == nacc - 1) {
+                    S += f2ll_bits(v[a][jj]);               // lumped orders >= 6
+                  } else {
+                    // exact order t: the value is m 2^(56-7t) with |m| < 2^24
+                    const int t = a <= 3 ? a + 2 : 5;
+                    const float sc = __int_as_float((127 + 7 * t - 56) << 23);
+                    S += (long long)__float2int_rz(__uint_as_float(v[a][jj]) * sc) << (49 - 7 * t);
+                  }
+                }
                 const double val = assemble(S, er + expB[j] - 1070);
                 const size_t idx = (size_t)row + (size_t)j * N;
                 double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
