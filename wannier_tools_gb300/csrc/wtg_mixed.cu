@@ -687,7 +687,7 @@ __device__ __forceinline__ float2 shfl_f2c(float2 v, int src) {
 // step k's pivot data from column k's values x (after step k-1): pivot row,
 // reciprocal, and the multiplier column (column k with rows k and p swapped)
 // into cb; sets misc[1] on an exact zero pivot
-__device__ __noinline__ void gj_pivot_publish(const float2 (&x)[4], int k, int N, float2* cb,
+__device__ __forceinline__ void gj_pivot_publish(const float2 (&x)[4], int k, int N, float2* cb,
                                               float2* recip, int* perm, int* misc) {
   const int lane = threadIdx.x & 31;
   long long best;
@@ -719,7 +719,7 @@ __device__ __noinline__ void gj_pivot_publish(const float2 (&x)[4], int k, int N
 // (look-ahead) and publishes its multiplier column into the other of two
 // buffers, so a step needs one barrier.  Same operations per entry as the
 // step-by-step form.
-__device__ int gj32_start(const double2* __restrict__ X, double2 w, int N, double2* Mi,
+__device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w, int N, double2* Mi,
                           double2* G, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
@@ -863,7 +863,7 @@ __device__ __forceinline__ int gj_argmax_r(const float2 (&x)[R], int k, int N, l
 }
 
 // gj_pivot_publish for a column of MX_ROWS rows per lane; the reciprocal goes to *rslot
-__device__ __noinline__ void gj_pivot_publish_r(const float2 (&x)[MX_ROWS], int k, int N,
+__device__ __forceinline__ void gj_pivot_publish_r(const float2 (&x)[MX_ROWS], int k, int N,
                                                 float2* cb, float2* rslot, int* perm, int* misc) {
   const int lane = threadIdx.x & 31;
   long long best;
@@ -916,7 +916,7 @@ __device__ __forceinline__ void gj_step_col(float2 (&x)[MX_ROWS], const float2* 
 // multiplier column (look-ahead).  Then every other column is read once into
 // registers, put through the panel's steps in order and written back.  Same
 // operations per entry as gj32_start.
-__device__ int gj32_global(const double2* __restrict__ X, double2 w, int N, double2* Mi,
+__device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w, int N, double2* Mi,
                            double2* G, float2* __restrict__ Wf, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
