@@ -6,9 +6,13 @@ every call raises; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libwtgpu.so"
+# the in-tree build; WTG_LIBRARY names another build of the same library (an
+# experimental or instrumented build) to load instead
+LIB_PATH = Path(os.environ["WTG_LIBRARY"]) if os.environ.get("WTG_LIBRARY") else \
+    Path(__file__).resolve().parent / "libwtgpu.so"
 
 WTG_OK = 0
 WTG_EINVAL = -1
