@@ -68,7 +68,7 @@ constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident c
 // that order 5 is split over two K halves (nacc = 6), since 4 * 127^2 * K must
 // stay below 2^24.
 struct MxPlan {
-  int N, NP, nrb, nacc, both, ncb, w0;
+  int N, NP, nrb, nacc, ncb, w0;
   int wb;                    // B-plane width of the shared-memory layout (>= w0)
 };
 
@@ -83,7 +83,6 @@ __host__ __device__ inline MxPlan mx_plan(int N) {
   p.ncb = (p.NP + wmax - 1) / wmax;
   p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 7) & ~7;
   while (p.ncb > 1 && (p.ncb - 1) * p.w0 >= p.NP) --p.ncb;
-  p.both = 1;
   p.wb = p.w0;
   return p;
 }
@@ -217,8 +216,8 @@ __device__ __forceinline__ double f2d_bits(float f) {     // exact FP32 -> FP64
 struct MxShared {
   unsigned char* buf[2];   // per buffer: 2*NSL A planes then 2*NSL B planes
   float2* gj;              // FP32 Gauss-Jordan matrix (aliases the buffers)
-  float2* pan;             // [N][MX_PANEL] panel of the global-memory Gauss-Jordan (aliases)
-  float2* mult;            // [N][MX_PANEL] its multiplier columns (aliases)
+  float2* mult;            // [MX_MAXN][MX_PANEL] multiplier columns of the global-memory
+                           // Gauss-Jordan's panel (aliases the buffers)
   float2* colbuf;
   float2* rowbuf;
   float2* recip;
@@ -244,8 +243,7 @@ __device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int WB) {
   s.buf[0] = smraw;
   s.buf[1] = smraw + bb;
   s.gj = reinterpret_cast<float2*>(smraw);
-  s.pan = reinterpret_cast<float2*>(smraw);
-  s.mult = s.pan + (size_t)MX_MAXN * MX_PANEL;
+  s.mult = reinterpret_cast<float2*>(smraw);
   unsigned char* tail = smraw + 2 * bb;
   s.colbuf = reinterpret_cast<float2*>(tail);
   s.rowbuf = s.colbuf + MX_MAXN;
@@ -497,7 +495,6 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
   for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
     const int rb0 = rb * 128;
     for (int pass = 0; pass < npass && !st.abort; ++pass) {
-      const int comp0 = 0, comp1 = 1;
       const int cbi = pass;
       const int jb = cbi * pl.w0;
       const int width = min(pl.w0, pl.NP - jb);
@@ -530,7 +527,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
       st.abort = __syncthreads_or(st.abort);
       tc_fence_after();
       const int* __restrict__ expB = s.expB;
-      for (int comp = comp0; comp <= comp1 && !st.abort; ++comp) {
+      for (int comp = 0; comp < 2 && !st.abort; ++comp) {
         const int warp = tid >> 5, lane = tid & 31;
         const int quad = warp & 3, hw = warp >> 2;
         const int row = rb0 + quad * 32 + lane;
@@ -1327,7 +1324,7 @@ size_t mixed_smem(int N, int wb = 0) {
   const MxPlan pl = mx_plan(N);
   const size_t bufbytes = (size_t)bufbytes_of(wb > 0 ? wb : pl.w0);
   // the FP32 Gauss-Jordan matrix ((N+1)*N float2, Ndim <= MX_SMEM_GJ_N) or the
-  // panel and multiplier columns (2 * N * MX_PANEL float2) alias the buffers
+  // multiplier columns (MX_MAXN * MX_PANEL float2, reserved twice) alias the buffers
   size_t planes = 2 * bufbytes;
   const size_t gj = N <= MX_SMEM_GJ_N ? (size_t)(N + 1) * N * 8 : (size_t)2 * MX_MAXN * MX_PANEL * 8;
   if (gj > planes) planes = gj;
