@@ -259,6 +259,15 @@ __device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int WB) {
   return s;
 }
 
+// a pointer into the dynamic shared memory, re-derived from the shared array
+// itself so that accesses through it compile to shared-memory instructions
+// (pointers read back from MxShared are generic)
+template <class T>
+__device__ __forceinline__ T* shm(const MxShared& s, T* p) {
+  extern __shared__ __align__(1024) unsigned char smem_dyn[];
+  return reinterpret_cast<T*>(smem_dyn + (reinterpret_cast<const unsigned char*>(p) - s.buf[0]));
+}
+
 struct MxState {           // per-thread copies of the (uniform) pipeline counters
   uint32_t tmem;
   uint32_t ncommit[2];
@@ -399,10 +408,10 @@ __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigne
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
                             int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b,
                             int gtid, int gthreads) {
-  unsigned char* __restrict__ A = s.buf[b];
+  unsigned char* __restrict__ A = shm(s, s.buf[b]);
   unsigned char* __restrict__ B = A + 2 * NSL * APLANE;
-  const int* __restrict__ expA = s.expA;
-  const int* __restrict__ expB = s.expB;
+  const int* __restrict__ expA = shm(s, s.expA);
+  const int* __restrict__ expB = shm(s, s.expB);
   const int bstride = width * KCH * 2 / 4;        // B plane stride in words (= pass width)
   for (int it = gtid; it < 128 * (KCH / 2); it += gthreads) {
     const int cm = it >> 5, ln = it & 31;
@@ -526,7 +535,8 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
       }
       st.abort = __syncthreads_or(st.abort);
       tc_fence_after();
-      const int* __restrict__ expB = s.expB;
+      const int* __restrict__ expB = shm(s, s.expB);
+      const int* __restrict__ expA = shm(s, s.expA);
       for (int comp = 0; comp < 2 && !st.abort; ++comp) {
         const int warp = tid >> 5, lane = tid & 31;
         const int quad = warp & 3, hw = warp >> 2;
@@ -534,7 +544,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
         // a warp whose 32 tensor-memory lanes are all padding rows has nothing to drain
         const int nhw = blockDim.x >> 7;
         const int cb = hw * 4, ce = rb0 + quad * 32 < N ? width : 0;
-        const int er = row < N ? s.expA[row] : 0;
+        const int er = row < N ? expA[row] : 0;
         const uint32_t bank = (uint32_t)(comp * width);
         for (int c0 = cb; c0 < ce; c0 += 4 * nhw) {
           uint32_t v[6][4];
@@ -720,13 +730,15 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
                           double2* G, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
-  float2* __restrict__ sM = s_.gj;
-  float2* const cb0 = s_.colbuf;          // multiplier columns of even / odd steps
-  float2* const cb1 = s_.rowbuf;
-  float2* __restrict__ recip = s_.recip;
-  int* __restrict__ perm = s_.perm;
-  int* __restrict__ cols = s_.cols;
-  int* __restrict__ misc = s_.misc;
+  // pointers re-derived from the dynamic shared-memory array, so that the
+  // compiler emits shared-memory (not generic) loads and stores
+  float2* __restrict__ sM = shm(s_, s_.gj);
+  float2* const cb0 = shm(s_, s_.colbuf);   // multiplier columns of even / odd steps
+  float2* const cb1 = shm(s_, s_.rowbuf);
+  float2* __restrict__ recip = shm(s_, s_.recip);
+  int* __restrict__ perm = shm(s_, s_.perm);
+  int* __restrict__ cols = shm(s_, s_.cols);
+  int* __restrict__ misc = shm(s_, s_.misc);
   for (int j = warp; j < N; j += nwarp) {
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
@@ -917,11 +929,11 @@ __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w
                            double2* G, float2* __restrict__ Wf, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
-  float2* __restrict__ Cm = s_.mult;
-  float2* __restrict__ recip = s_.recip;
-  int* __restrict__ perm = s_.perm;
-  int* __restrict__ cols = s_.cols;
-  int* __restrict__ misc = s_.misc;
+  float2* __restrict__ Cm = shm(s_, s_.mult);
+  float2* __restrict__ recip = shm(s_, s_.recip);
+  int* __restrict__ perm = shm(s_, s_.perm);
+  int* __restrict__ cols = shm(s_, s_.cols);
+  int* __restrict__ misc = shm(s_, s_.misc);
   for (int j = warp; j < N; j += nwarp) {
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
