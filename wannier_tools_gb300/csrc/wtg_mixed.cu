@@ -228,7 +228,7 @@ struct MxShared {
   float* red;              // [32]
   uint64_t* mbar;          // [2]
   uint32_t* tslot;
-  int* misc;               // 0 instance, 1 singular, 2 abort
+  int* misc;               // 0 instance, 1 singular, 2-3 pivot rows (shared-memory Gauss-Jordan)
 };
 
 __host__ __device__ __forceinline__ int bufbytes_of(int WB) {
@@ -645,39 +645,6 @@ __device__ float block_sum_f(float v, MxShared& s) {
   return t;
 }
 
-__device__ __forceinline__ long long cabs1_key_f(float2 v) {
-  return (long long)__float_as_uint(fabsf(v.x) + fabsf(v.y));
-}
-
-// pivot over rows >= k of the column values x (rows lane + 32 m): the first
-// maximal |re| + |im| (izamax's rule); warp-uniform result and key
-__device__ __forceinline__ int gj_argmax4(const float2 (&x)[4], int k, int N, long long& best) {
-  const int lane = threadIdx.x & 31;
-  best = -1;
-  int bi = N;
-#pragma unroll
-  for (int m = 0; m < 4; ++m) {
-    const int i = lane + 32 * m;
-    if (i >= k && i < N) {
-      const long long v = cabs1_key_f(x[m]);
-      if (v > best) {
-        best = v;
-        bi = i;
-      }
-    }
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
-    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-    if (ob > best || (ob == best && oi < bi)) {
-      best = ob;
-      bi = oi;
-    }
-  }
-  return bi;
-}
-
 // entry m (warp-uniform) of a 4-entry register column, without local memory
 __device__ __forceinline__ float2 pick4(const float2 (&x)[4], int m) {
   float2 v = x[0];
@@ -691,28 +658,62 @@ __device__ __forceinline__ float2 shfl_f2c(float2 v, int src) {
   return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-// step k's pivot data from column k's values x (after step k-1): pivot row,
-// reciprocal, and the multiplier column (column k with rows k and p swapped)
-// into cb; sets misc[1] on an exact zero pivot
-__device__ __forceinline__ void gj_pivot_publish(const float2 (&x)[4], int k, int N, float2* cb,
-                                              float2* recip, int* perm, int* misc) {
+// Gauss-Jordan without physical row swaps: row i of the working matrix stays
+// in place and pos_of[i] / row_at[q] record the position it would hold in the
+// swapped form.  Step t's pivot is the first maximal |re| + |im| of column t
+// over the rows at positions >= t (izamax's rule in position order), so the
+// pivots, and every FMA of every entry, are those of the swapped form; only
+// the storage order differs.  Publishes the multiplier column (column t as it
+// stands), the pivot's position (perm[t]) and physical row (misc[2 + (t & 1)])
+// and its reciprocal, and moves the pivot to position t.
+__device__ __forceinline__ void gj_pivot_publish_u(const float2 (&x)[4], int t, int N, float2* cb,
+                                                float2* recip, int* perm, int* misc, int* pos_of,
+                                                int* row_at) {
   const int lane = threadIdx.x & 31;
-  long long best;
-  const int p = gj_argmax4(x, k, N, best);
-  const float2 xk = shfl_f2c(pick4(x, k >> 5), k & 31);
-  const float2 xp = shfl_f2c(pick4(x, p >> 5), p & 31);
+  int bkey = -1, bpos = 0x7fffffff, brow = N;
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
     const int i = lane + 32 * m;
-    if (i < N) cb[i] = (i == p) ? xk : x[m];
+    if (i < N) {
+      const int ps = pos_of[i];
+      const int key = __float_as_int(fabsf(x[m].x) + fabsf(x[m].y));
+      if (ps >= t && (key > bkey || (key == bkey && ps < bpos))) {
+        bkey = key;
+        bpos = ps;
+        brow = i;
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const int ok = __shfl_xor_sync(0xffffffffu, bkey, off);
+    const int op = __shfl_xor_sync(0xffffffffu, bpos, off);
+    const int orow = __shfl_xor_sync(0xffffffffu, brow, off);
+    if (ok > bkey || (ok == bkey && op < bpos)) {
+      bkey = ok;
+      bpos = op;
+      brow = orow;
+    }
+  }
+  const float2 xp = shfl_f2c(pick4(x, brow >> 5), brow & 31);
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int i = lane + 32 * m;
+    if (i < N) cb[i] = x[m];
   }
   if (lane == 0) {
-    perm[k] = p;
-    if (best == 0) {
+    perm[t] = bpos;
+    misc[2 + (t & 1)] = brow;
+    const int rk = row_at[t];            // the row at position t moves to the pivot's position
+    row_at[bpos] = rk;
+    pos_of[rk] = bpos;
+    row_at[t] = brow;
+    pos_of[brow] = t;
+    if (bkey == 0) {
       misc[1] = 1;
     } else {
       const float inv_d = 1.0f / (xp.x * xp.x + xp.y * xp.y);
-      recip[k & 1] = make_float2(xp.x * inv_d, -xp.y * inv_d);
+      recip[t & 1] = make_float2(xp.x * inv_d, -xp.y * inv_d);
     }
   }
 }
@@ -720,12 +721,14 @@ __device__ __forceinline__ void gj_pivot_publish(const float2 (&x)[4], int k, in
 // M = w I - X (FP64, kept in Mi for the refinement), then FP32 Gauss-Jordan
 // into G (FP64).  Returns 1 on an exact zero pivot (G = identity then).
 // Ndim <= 112.  Each pivot step is one pass in which every warp takes whole
-// columns into registers (lane l holds rows l, l+32, ...): the row swap, the
-// pivot-row scaling and the elimination of a column happen in registers with
-// two shuffles.  The warp that owns column k+1 also finds step k+1's pivot
+// columns into registers (lane l holds rows l, l+32, ...): the pivot-row
+// scaling and the elimination of a column happen in registers with one
+// shuffle pair.  Rows stay in place (gj_pivot_publish_u), so an entry needs
+// one select besides its four FMAs; the output reads the rows back in pivot
+// order.  The warp that owns column k+1 also finds step k+1's pivot
 // (look-ahead) and publishes its multiplier column into the other of two
 // buffers, so a step needs one barrier.  Same operations per entry as the
-// step-by-step form.
+// step-by-step form with row swaps.
 __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w, int N, double2* Mi,
                           double2* G, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
@@ -739,6 +742,8 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
   int* __restrict__ perm = shm(s_, s_.perm);
   int* __restrict__ cols = shm(s_, s_.cols);
   int* __restrict__ misc = shm(s_, s_.misc);
+  int* __restrict__ pos_of = shm(s_, s_.expA);   // the exponent arrays are free here
+  int* __restrict__ row_at = shm(s_, s_.expB);
   for (int j = warp; j < N; j += nwarp) {
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
@@ -749,6 +754,10 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
       sM[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
     }
   }
+  for (int i = tid; i < N; i += T) {
+    pos_of[i] = i;
+    row_at[i] = i;
+  }
   if (tid == 0) misc[1] = 0;
   __syncthreads();
   if (warp == 0) {                        // step 0's pivot
@@ -758,12 +767,12 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
       const int i = lane + 32 * m;
       x[m] = i < N ? sM[i] : make_float2(0.f, 0.f);
     }
-    gj_pivot_publish(x, 0, N, cb0, recip, perm, misc);
+    gj_pivot_publish_u(x, 0, N, cb0, recip, perm, misc, pos_of, row_at);
   }
   __syncthreads();
   for (int k = 0; k < N; ++k) {
     if (misc[1]) break;
-    const int p = perm[k];
+    const int p = misc[2 + (k & 1)];        // the pivot's row
     const float2 r = recip[k & 1];
     const float2* cb = (k & 1) ? cb1 : cb0;
     float2* cbn = (k & 1) ? cb0 : cb1;
@@ -781,24 +790,26 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
         const int i = lane + 32 * m;
         x[m] = i < N ? col[i] : make_float2(0.f, 0.f);
       }
-      const float2 akj = shfl_f2c(pick4(x, k >> 5), k & 31);
-      const float2 apj = shfl_f2c(pick4(x, p >> 5), p & 31);
-      const bool jk = j == k;
-      const float2 nk = jk ? r
-                           : make_float2(fmaf(apj.x, r.x, -apj.y * r.y),
-                                         fmaf(apj.x, r.y, apj.y * r.x));
+      float2 nk = r;
+      if (j == k) {                       // the pivot column becomes a column of the inverse
+#pragma unroll
+        for (int m = 0; m < 4; ++m) x[m] = make_float2(0.f, 0.f);
+      } else {
+        const float2 apj = shfl_f2c(pick4(x, p >> 5), p & 31);
+        nk = make_float2(fmaf(apj.x, r.x, -apj.y * r.y), fmaf(apj.x, r.y, apj.y * r.x));
+      }
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         const int i = lane + 32 * m;
-        float2 v = jk ? make_float2(0.f, 0.f) : ((i == p) ? akj : x[m]);
+        float2 v = x[m];
         v.x = fmaf(-f[m].x, nk.x, v.x);
         v.x = fmaf(f[m].y, nk.y, v.x);
         v.y = fmaf(-f[m].x, nk.y, v.y);
         v.y = fmaf(-f[m].y, nk.x, v.y);
-        x[m] = (i == k) ? nk : v;
+        x[m] = (i == p) ? nk : v;
         if (i < N) col[i] = x[m];
       }
-      if (j == k + 1) gj_pivot_publish(x, k + 1, N, cbn, recip, perm, misc);
+      if (j == k + 1) gj_pivot_publish_u(x, k + 1, N, cbn, recip, perm, misc, pos_of, row_at);
     }
     __syncthreads();
   }
@@ -822,7 +833,7 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
       if (singular) {
         G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
       } else {
-        const float2 v = sM[i + (size_t)cj * N];
+        const float2 v = sM[row_at[i] + (size_t)cj * N];
         G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
       }
     }
@@ -831,10 +842,11 @@ __device__ __noinline__ int gj32_start(const double2* __restrict__ X, double2 w,
   return singular;
 }
 
-__device__ __forceinline__ float2 pick_f(const float2 (&x)[MX_ROWS], int m) {
+template <int R>
+__device__ __forceinline__ float2 pick_f(const float2 (&x)[R], int m) {
   float2 v = x[0];
 #pragma unroll
-  for (int q = 1; q < MX_ROWS; ++q)
+  for (int q = 1; q < R; ++q)
     if (q == m) v = x[q];
   return v;
 }
@@ -843,50 +855,54 @@ __device__ __forceinline__ float2 shfl_f2(float2 v, int src) {
   return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
+// gj_pivot_publish_u for a column of R rows per lane (rows lane + 32 m): the
+// multiplier column goes to cb, the reciprocal to *rslot, the pivot's row to
+// prow[t]
 template <int R>
-__device__ __forceinline__ int gj_argmax_r(const float2 (&x)[R], int k, int N, long long& best) {
+__device__ __forceinline__ void gj_pivot_publish_ur(const float2 (&x)[R], int t, int N, float2* cb,
+                                                 float2* rslot, int* perm, int* prow, int* misc,
+                                                 int* pos_of, int* row_at) {
   const int lane = threadIdx.x & 31;
-  best = -1;
-  int bi = N;
+  int bkey = -1, bpos = 0x7fffffff, brow = N;
 #pragma unroll
   for (int m = 0; m < R; ++m) {
     const int i = lane + 32 * m;
-    if (i >= k && i < N) {
-      const long long v = cabs1_key_f(x[m]);
-      if (v > best) {
-        best = v;
-        bi = i;
+    if (i < N) {
+      const int ps = pos_of[i];
+      const int key = __float_as_int(fabsf(x[m].x) + fabsf(x[m].y));
+      if (ps >= t && (key > bkey || (key == bkey && ps < bpos))) {
+        bkey = key;
+        bpos = ps;
+        brow = i;
       }
     }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
-    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-    if (ob > best || (ob == best && oi < bi)) {
-      best = ob;
-      bi = oi;
+    const int ok = __shfl_xor_sync(0xffffffffu, bkey, off);
+    const int op = __shfl_xor_sync(0xffffffffu, bpos, off);
+    const int orow = __shfl_xor_sync(0xffffffffu, brow, off);
+    if (ok > bkey || (ok == bkey && op < bpos)) {
+      bkey = ok;
+      bpos = op;
+      brow = orow;
     }
   }
-  return bi;
-}
-
-// gj_pivot_publish for a column of MX_ROWS rows per lane; the reciprocal goes to *rslot
-__device__ __forceinline__ void gj_pivot_publish_r(const float2 (&x)[MX_ROWS], int k, int N,
-                                                float2* cb, float2* rslot, int* perm, int* misc) {
-  const int lane = threadIdx.x & 31;
-  long long best;
-  const int p = gj_argmax_r<MX_ROWS>(x, k, N, best);
-  const float2 xk = shfl_f2(pick_f(x, k >> 5), k & 31);
-  const float2 xp = shfl_f2(pick_f(x, p >> 5), p & 31);
+  const float2 xp = shfl_f2(pick_f<R>(x, brow >> 5), brow & 31);
 #pragma unroll
-  for (int m = 0; m < MX_ROWS; ++m) {
+  for (int m = 0; m < R; ++m) {
     const int i = lane + 32 * m;
-    if (i < N) cb[i] = (i == p) ? xk : x[m];
+    if (i < N) cb[i] = x[m];
   }
   if (lane == 0) {
-    perm[k] = p;
-    if (best == 0) {
+    perm[t] = bpos;
+    prow[t] = brow;
+    const int rk = row_at[t];
+    row_at[bpos] = rk;
+    pos_of[rk] = bpos;
+    row_at[t] = brow;
+    pos_of[brow] = t;
+    if (bkey == 0) {
       misc[1] = 1;
     } else {
       const float inv_d = 1.0f / (xp.x * xp.x + xp.y * xp.y);
@@ -896,35 +912,41 @@ __device__ __forceinline__ void gj_pivot_publish_r(const float2 (&x)[MX_ROWS], i
 }
 
 // one Gauss-Jordan step k (pivot row p, reciprocal r, multiplier column cm in
-// shared memory) applied to column j held in registers
-__device__ __forceinline__ void gj_step_col(float2 (&x)[MX_ROWS], const float2* __restrict__ cm,
-                                            int N, int j, int k, int p, float2 r) {
+// shared memory) applied to column j held in registers, rows in place
+template <int R>
+__device__ __forceinline__ void gj_step_col_u(float2 (&x)[R], const float2* __restrict__ cm, int N,
+                                              int j, int k, int p, float2 r) {
   const int lane = threadIdx.x & 31;
-  const float2 akj = shfl_f2(pick_f(x, k >> 5), k & 31);
-  const float2 apj = shfl_f2(pick_f(x, p >> 5), p & 31);
-  const bool jk = j == k;
-  const float2 nk = jk ? r : make_float2(fmaf(apj.x, r.x, -apj.y * r.y), fmaf(apj.x, r.y, apj.y * r.x));
+  float2 nk = r;
+  if (j == k) {
 #pragma unroll
-  for (int m = 0; m < MX_ROWS; ++m) {
+    for (int m = 0; m < R; ++m) x[m] = make_float2(0.f, 0.f);
+  } else {
+    const float2 apj = shfl_f2(pick_f<R>(x, p >> 5), p & 31);
+    nk = make_float2(fmaf(apj.x, r.x, -apj.y * r.y), fmaf(apj.x, r.y, apj.y * r.x));
+  }
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
     const int i = lane + 32 * m;
     const float2 f = i < N ? cm[i] : make_float2(0.f, 0.f);
-    float2 v = jk ? make_float2(0.f, 0.f) : ((i == p) ? akj : x[m]);
+    float2 v = x[m];
     v.x = fmaf(-f.x, nk.x, v.x);
     v.x = fmaf(f.y, nk.y, v.x);
     v.y = fmaf(-f.x, nk.y, v.y);
     v.y = fmaf(-f.y, nk.x, v.y);
-    x[m] = (i == k) ? nk : v;
+    x[m] = (i == p) ? nk : v;
   }
 }
 
 // As gj32_start for Ndim above the shared-memory limit: the FP32 matrix lives
 // in global memory (Wf, N x N float2) and the pivot steps run in panels of
 // MX_PANEL columns.  A panel's columns stay in registers (warp w owns panel
-// columns w and w + 8, lane l rows l, l+32, ...); each step updates them with
+// column w, lane l rows l, l+32, ..., R rows per lane); each step updates them with
 // one barrier, the owner of the next column publishing the next pivot and its
 // multiplier column (look-ahead).  Then every other column is read once into
-// registers, put through the panel's steps in order and written back.  Same
-// operations per entry as gj32_start.
+// registers, put through the panel's steps in order and written back.  Rows
+// stay in place as in gj32_start.
+template <int R>
 __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w, int N, double2* Mi,
                            double2* G, float2* __restrict__ Wf, MxShared& s_) {
   const int T = blockDim.x, tid = threadIdx.x;
@@ -934,6 +956,9 @@ __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w
   int* __restrict__ perm = shm(s_, s_.perm);
   int* __restrict__ cols = shm(s_, s_.cols);
   int* __restrict__ misc = shm(s_, s_.misc);
+  int* const prow = cols;                        // pivot rows during the steps
+  int* __restrict__ pos_of = shm(s_, s_.expA);   // the exponent arrays are free here
+  int* __restrict__ row_at = shm(s_, s_.expB);
   for (int j = warp; j < N; j += nwarp) {
     for (int i = lane; i < N; i += 32) {
       const size_t e = (size_t)i + (size_t)j * N;
@@ -944,32 +969,38 @@ __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w
       Wf[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
     }
   }
+  for (int i = tid; i < N; i += T) {
+    pos_of[i] = i;
+    row_at[i] = i;
+  }
   if (tid == 0) misc[1] = 0;
   __syncthreads();
   for (int k0 = 0; k0 < N; k0 += MX_PANEL) {
     const int pb = min(MX_PANEL, N - k0);
-    float2 xc[2][MX_ROWS];                // this warp's panel columns warp, warp + nwarp
+    float2 xc[2][R];                // this warp's panel columns warp, warp + nwarp
 #pragma unroll
     for (int cc = 0; cc < 2; ++cc) {
       const int c = warp + cc * nwarp;
 #pragma unroll
-      for (int m = 0; m < MX_ROWS; ++m) {
+      for (int m = 0; m < R; ++m) {
         const int i = lane + 32 * m;
         xc[cc][m] = (c < pb && i < N) ? Wf[(size_t)(k0 + c) * N + i] : make_float2(0.f, 0.f);
       }
     }
-    if (warp == 0) gj_pivot_publish_r(xc[0], k0, N, Cm, &recip[0], perm, misc);
+    if (warp == 0) gj_pivot_publish_ur<R>(xc[0], k0, N, Cm, &recip[0], perm, prow, misc, pos_of, row_at);
     __syncthreads();
     for (int t = 0; t < pb; ++t) {
       if (misc[1]) break;
-      const int k = k0 + t, p = perm[k];
+      const int k = k0 + t, p = prow[k];
       const float2 r = recip[t];
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
         const int c = warp + cc * nwarp;
         if (c < pb) {
-          gj_step_col(xc[cc], Cm + t * N, N, k0 + c, k, p, r);
-          if (c == t + 1) gj_pivot_publish_r(xc[cc], k + 1, N, Cm + (t + 1) * N, &recip[t + 1], perm, misc);
+          gj_step_col_u<R>(xc[cc], Cm + t * N, N, k0 + c, k, p, r);
+          if (c == t + 1)
+            gj_pivot_publish_ur<R>(xc[cc], k + 1, N, Cm + (t + 1) * N, &recip[t + 1], perm, prow, misc,
+                                   pos_of, row_at);
         }
       }
       __syncthreads();
@@ -980,7 +1011,7 @@ __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w
       const int c = warp + cc * nwarp;
       if (c < pb) {
 #pragma unroll
-        for (int m = 0; m < MX_ROWS; ++m) {
+        for (int m = 0; m < R; ++m) {
           const int i = lane + 32 * m;
           if (i < N) Wf[(size_t)(k0 + c) * N + i] = xc[cc][m];
         }
@@ -990,15 +1021,15 @@ __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w
     for (int j = warp; j < N; j += nwarp) {
       if (j >= k0 && j < k0 + pb) continue;
       float2* col = Wf + (size_t)j * N;
-      float2 x[MX_ROWS];
+      float2 x[R];
 #pragma unroll
-      for (int q = 0; q < MX_ROWS; ++q) {
+      for (int q = 0; q < R; ++q) {
         const int i = lane + 32 * q;
         x[q] = i < N ? col[i] : make_float2(0.f, 0.f);
       }
-      for (int t = 0; t < pb; ++t) gj_step_col(x, Cm + t * N, N, j, k0 + t, perm[k0 + t], recip[t]);
+      for (int t = 0; t < pb; ++t) gj_step_col_u<R>(x, Cm + t * N, N, j, k0 + t, prow[k0 + t], recip[t]);
 #pragma unroll
-      for (int q = 0; q < MX_ROWS; ++q) {
+      for (int q = 0; q < R; ++q) {
         const int i = lane + 32 * q;
         if (i < N) col[i] = x[q];
       }
@@ -1025,7 +1056,7 @@ __device__ __noinline__ int gj32_global(const double2* __restrict__ X, double2 w
       if (singular) {
         G[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
       } else {
-        const float2 v = Wf[i + (size_t)cj * N];
+        const float2 v = Wf[row_at[i] + (size_t)cj * N];
         G[e] = make_double2(f2d_bits(v.x), f2d_bits(v.y));
       }
     }
@@ -1044,8 +1075,11 @@ __device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int 
                              double2** Gp, double2** Gnp, double2* Mi, double2* R, MxShared& s,
                              MxState& st, float brk = 1e-7f) {
   const int N = pl.N;
+  float2* const Wf = reinterpret_cast<float2*>(R);
   const int sing = N <= MX_SMEM_GJ_N ? gj32_start(X, w, N, Mi, *Gp, s)
-                                     : gj32_global(X, w, N, Mi, *Gp, reinterpret_cast<float2*>(R), s);
+                   : N <= 160        ? gj32_global<5>(X, w, N, Mi, *Gp, Wf, s)
+                   : N <= 224        ? gj32_global<7>(X, w, N, Mi, *Gp, Wf, s)
+                                     : gj32_global<MX_ROWS>(X, w, N, Mi, *Gp, Wf, s);
   float prev = 3.0e38f;
   for (int t = 0; t < ns_max && !st.abort; ++t) {
     const float part = oz_gemm<OZ_IMINUS>(Mi, *Gp, pl, R, nullptr, nullptr, s, st);  // R = I - M G
