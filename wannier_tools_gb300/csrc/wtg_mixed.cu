@@ -684,16 +684,14 @@ __device__ __forceinline__ void gj_pivot_publish_u(const float2 (&x)[4], int t, 
       }
     }
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const int ok = __shfl_xor_sync(0xffffffffu, bkey, off);
-    const int op = __shfl_xor_sync(0xffffffffu, bpos, off);
-    const int orow = __shfl_xor_sync(0xffffffffu, brow, off);
-    if (ok > bkey || (ok == bkey && op < bpos)) {
-      bkey = ok;
-      bpos = op;
-      brow = orow;
-    }
+  {  // warp maximum of the key, then the smallest position among the lanes that hold it
+    const unsigned kmax = __reduce_max_sync(0xffffffffu, (unsigned)(bkey + 1));
+    const bool cand = (unsigned)(bkey + 1) == kmax;
+    const int pmin = (int)__reduce_min_sync(0xffffffffu, cand ? (unsigned)bpos : 0xffffffffu);
+    const int src = __ffs(__ballot_sync(0xffffffffu, cand && bpos == pmin)) - 1;
+    brow = __shfl_sync(0xffffffffu, brow, src);
+    bkey = (int)kmax - 1;
+    bpos = pmin;
   }
   const float2 xp = shfl_f2c(pick4(x, brow >> 5), brow & 31);
 #pragma unroll
@@ -877,16 +875,14 @@ __device__ __forceinline__ void gj_pivot_publish_ur(const float2 (&x)[R], int t,
       }
     }
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const int ok = __shfl_xor_sync(0xffffffffu, bkey, off);
-    const int op = __shfl_xor_sync(0xffffffffu, bpos, off);
-    const int orow = __shfl_xor_sync(0xffffffffu, brow, off);
-    if (ok > bkey || (ok == bkey && op < bpos)) {
-      bkey = ok;
-      bpos = op;
-      brow = orow;
-    }
+  {  // warp maximum of the key, then the smallest position among the lanes that hold it
+    const unsigned kmax = __reduce_max_sync(0xffffffffu, (unsigned)(bkey + 1));
+    const bool cand = (unsigned)(bkey + 1) == kmax;
+    const int pmin = (int)__reduce_min_sync(0xffffffffu, cand ? (unsigned)bpos : 0xffffffffu);
+    const int src = __ffs(__ballot_sync(0xffffffffu, cand && bpos == pmin)) - 1;
+    brow = __shfl_sync(0xffffffffu, brow, src);
+    bkey = (int)kmax - 1;
+    bpos = pmin;
   }
   const float2 xp = shfl_f2(pick_f<R>(x, brow >> 5), brow & 31);
 #pragma unroll
