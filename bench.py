@@ -56,8 +56,6 @@ WORKLOADS = {
                    omega_range=(-1.0, 1.0), nomega=201,
                    desc="surfstat k-path x omega, synthetic Num_wann=20 Np=2 (Ndim=40), "
                         "101 k x 201 omega in [-1,1] eV, eta=1e-2 eV, tol=1e-10, FP64"),
-    # the large k-path x omega spectrum: 301 k x 501 omega at Ndim 264; one k point
-    # (501 solves) per step, a strided subset of omegas in the CPU sample
     # four models of Ndim 16, 40, 112, 264 interleaved in one persistent launch per step; each
     # model has 4096 random (k, omega) points, eta log-uniform in [1e-4, 1e-2] eV; a step is 256
     # points of each model (the next slice of the 4 x 4096 set)
@@ -73,9 +71,12 @@ WORKLOADS = {
                    desc="serving loop: 8 synthetic models Num_wann 8..150, Np 1..3 (Ndim 8..300), "
                         "Poisson requests of 50-400 (k,omega) points, random omega windows in "
                         "[-1,1] eV, eta log-uniform [1e-3,1e-2] eV"),
+    # the large k-path x omega spectrum: 301 k x 501 omega at Ndim 264; two k points
+    # (1002 solves = 6.6 waves of one solve per SM; one k point, 3.3 waves, left 18 % of the
+    # last wave idle) per step, a strided subset of omegas in the CPU sample
     "ss_n264": dict(nw=88, np_=3, seed=2026, nk1=301, nk2=None, omega_ev=None, eta_ev=1e-3,
                     divide_by_pi=False, tol=None, cpu_per_core=1, ref_per_core=1,
-                    omega_range=(-0.5, 0.5), nomega=501, step_k=1, cpu_omegas=6,
+                    omega_range=(-0.5, 0.5), nomega=501, step_k=2, cpu_omegas=6,
                     desc="surfstat k-path x omega, synthetic Num_wann=88 Np=3 (Ndim=264), "
                          "301 k x 501 omega in [-0.5,0.5] eV, eta=1e-3 eV"),
 }
