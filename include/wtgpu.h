@@ -322,6 +322,32 @@ int wtg_engine_run(wtg_engine_t engine, int npts, const int* point_model, const 
                    const double* omega, const double* eta, double tol, int itermax,
                    int divide_by_pi, double* dos_l, double* dos_r, double* dos_bulk, int* iters,
                    unsigned char* status);
+/*
+ * CUDA graphs (on by default; WTG_ENGINE_GRAPHS=0 in the environment turns them
+ * off for new engines): a run's copy-in, counter reset, batch kernel and
+ * copy-out are captured once per staging capacity (the powers of two from 64 up
+ * to max_points) and replayed with one cudaGraphLaunch; the point count and the
+ * run's scalars travel in the staged header.  Results are bit-identical with
+ * graphs on and off.  graphs = captured capacities, graph_launches = replays.
+ */
+int wtg_engine_set_graphs(wtg_engine_t engine, int on);
+int wtg_engine_graph_info(wtg_engine_t engine, int* graphs, long long* graph_launches);
+
+/*
+ * Tile table (the autotuner's output, wannier_tools_gb300/autotune.py): the
+ * launch shape the kernels use at a given Ndim.
+ *   WTG_PREC_FP64   value = threads per CTA of the per-model FP64 kernel, 128, 256
+ *                   or 512 (Ndim above the shared-memory inverse always uses 256)
+ *   WTG_PREC_MIXED  value = output-column pass width of the split-BF16 products, a
+ *                   multiple of 8 up to 48 (Ndim <= 256) or 40 (above)
+ * value 0 restores the built-in choice.  Results do not depend on the tile beyond
+ * the order of the convergence norm's block sum (every output element is summed in
+ * the same order; spectra agree to 1e-12).  Set tiles before creating engines
+ * (an engine keeps the widths it was created with); wtg_tile_get returns the
+ * value in use and the built-in one.  No counterpart in the reference.
+ */
+int wtg_tile_set(int precision, int ndim, int value);
+int wtg_tile_get(int precision, int ndim, int* value, int* builtin);
 
 /* One-shot: create an engine for these models and points, run, destroy. */
 int wtg_batch_spectrum(int nmodels, const wtg_model_t* models, int npts, const int* point_model,

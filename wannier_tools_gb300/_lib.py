@@ -6,6 +6,7 @@ every call raises; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 from pathlib import Path
 
@@ -65,6 +66,10 @@ SIGNATURES = {
                                      C.POINTER(_vp)]),
     "wtg_engine_destroy": (C.c_int, [_vp]),
     "wtg_engine_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), _ip, C.POINTER(C.c_longlong)]),
+    "wtg_engine_set_graphs": (C.c_int, [_vp, C.c_int]),
+    "wtg_engine_graph_info": (C.c_int, [_vp, _ip, C.POINTER(C.c_longlong)]),
+    "wtg_tile_set": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+    "wtg_tile_get": (C.c_int, [C.c_int, C.c_int, _ip, _ip]),
     "wtg_engine_run": (C.c_int, [_vp, C.c_int, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
                                   _dp, _dp, _dp, _i32p, _u8p]),
     "wtg_batch_spectrum": (C.c_int, [C.c_int, C.POINTER(_vp), C.c_int, _ip, _dp, _dp, _dp, C.c_double,
@@ -100,7 +105,24 @@ def load(path: Path | None = None) -> C.CDLL:
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    if os.environ.get("WTG_TILES", "1") != "0":
+        _install_tiles(lib)
     return lib
+
+
+def _install_tiles(lib) -> None:
+    """Put the autotuner's table (tiles.json beside this file) for the current
+    device into the library; nothing without a device or without an entry."""
+    buf = C.create_string_buffer(256)
+    if lib.wtg_device_info(buf, 256) != 0:
+        return
+    from .autotune import FORMS, TABLE, device_key, entries_for
+    if not TABLE.exists():
+        return
+    table = json.loads(TABLE.read_text())
+    for form, ent in entries_for(table, device_key(buf.value.decode())).items():
+        for ndim, v in ent.items():
+            check(lib.wtg_tile_set(FORMS[form], ndim, v))
 
 
 def last_error() -> str:

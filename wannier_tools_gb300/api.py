@@ -259,7 +259,8 @@ class Engine:
     of several models (uneven Ndim, eta per point) in one persistent launch.
     One engine runs one batch at a time; separate engines run concurrently."""
 
-    def __init__(self, models, tops, bots, precision: int = PREC_FP64, max_points: int = 4096):
+    def __init__(self, models, tops, bots, precision: int = PREC_FP64, max_points: int = 4096,
+                 graphs: bool | None = None):
         lib = _lib.load()
         self.models = list(models)
         self._ntop, self._top, self._nbot, self._bot = _lists(self.models, tops, bots)
@@ -272,6 +273,18 @@ class Engine:
         self._handle = h
         self.precision = int(precision)
         self.max_points = int(max_points)
+        if graphs is not None:
+            check(lib.wtg_engine_set_graphs(h, 1 if graphs else 0))
+
+    def set_graphs(self, on: bool):
+        """Replay runs from captured CUDA graphs (default) or launch them directly."""
+        check(_lib.load().wtg_engine_set_graphs(self._handle, 1 if on else 0))
+
+    def graph_info(self) -> dict:
+        g = C.c_int(0)
+        n = C.c_longlong(0)
+        check(_lib.load().wtg_engine_graph_info(self._handle, C.byref(g), C.byref(n)))
+        return {"graphs": int(g.value), "graph_launches": int(n.value)}
 
     def info(self) -> dict:
         b = C.c_longlong(0)
@@ -311,6 +324,20 @@ class Engine:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def set_tile(precision: int, ndim: int, value: int) -> None:
+    """Launch shape used at this Ndim (wtg_tile_set): FP64 threads per CTA, mixed pass
+    width; 0 restores the built-in choice."""
+    check(_lib.load().wtg_tile_set(int(precision), int(ndim), int(value)))
+
+
+def get_tile(precision: int, ndim: int) -> tuple[int, int]:
+    """(value in use, built-in value) at this Ndim (wtg_tile_get)."""
+    v = C.c_int(0)
+    b = C.c_int(0)
+    check(_lib.load().wtg_tile_get(int(precision), int(ndim), C.byref(v), C.byref(b)))
+    return int(v.value), int(b.value)
 
 
 def batch_spectrum(models, tops, bots, point_model, kpts, omega, eta, tol: float = ACCURACY_REF,

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -169,6 +170,7 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
   a.status = d_st;
   a.ws = (double2*)m->ws.p;
   a.KC = cfg.KC;
+  a.w0 = cfg.w0;
   a.ntop = ntop;
   a.nbot = nbot;
   for (int q = 0; q < ntop; ++q) a.top[q] = top[q];
@@ -252,6 +254,21 @@ int count_flagged(const uint8_t* st, size_t n) {
 // sized for their largest Ndim, its own stream and staging.  One engine runs
 // one batch at a time (calls are serialised by its mutex); several engines
 // run concurrently on one device.
+namespace wtg {
+namespace {
+std::atomic<int> g_tiles[2][TILE_MAX_N + 1];
+}  // namespace
+
+int tile_value(int precision, int N) {
+  if (precision < 0 || precision > 1 || N < 1 || N > TILE_MAX_N) return 0;
+  return g_tiles[precision][N].load(std::memory_order_relaxed);
+}
+
+void tile_store(int precision, int N, int value) {
+  g_tiles[precision][N].store(value, std::memory_order_relaxed);
+}
+}  // namespace wtg
+
 struct wtg_engine {
   int device = 0;
   int precision = 0;
@@ -271,11 +288,16 @@ struct wtg_engine {
   std::mutex mu;
   long long launches = 0;
   size_t device_bytes = 0;
+  // captured runs, one per staging capacity (powers of two up to max_points)
+  bool use_graphs = true;
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+  long long graph_launches = 0;
   ~wtg_engine() {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     models_d.release();
     lists_d.release();
     ws.release();
@@ -291,7 +313,10 @@ namespace {
 
 // per-point input block (device and pinned host): pmodel, order, k (npts x 2), omega, eta;
 // output block: dos_l, dos_r, dos_bulk, iters, status
-size_t engine_in_bytes(int n) { return (size_t)n * (4 + 4 + 16 + 8 + 8); }
+// input staging of capacity n: the run header (BatchRunHeader, 32 bytes) | pmodel |
+// order | k (n x 2) | omega | eta; output: dos_l | dos_r | dos_bulk | iters | status
+constexpr size_t RUN_HDR = sizeof(wtg::BatchRunHeader);
+size_t engine_in_bytes(int n) { return RUN_HDR + (size_t)n * (4 + 4 + 16 + 8 + 8); }
 size_t engine_out_bytes(int n) { return (size_t)n * (8 * 3 + 4 + 1); }
 
 int engine_create(int nmodels, const wtg_model_t* models, int precision, int max_points,
@@ -339,10 +364,13 @@ int engine_create(int nmodels, const wtg_model_t* models, int precision, int max
   const size_t ph_bytes = (size_t)max_nru * sizeof(double2);
   cudaError_t ce;
   if (mixed) {
-    ce = wtg::batch_mixed_config(max_n, &e->wb, &e->cfg);
+    ce = wtg::batch_mixed_prepare();
+    if (ce == cudaSuccess) ce = wtg::batch_mixed_config(max_n, &e->wb, &e->cfg);
   } else {
-    ce = wtg::batch_fp64_config(max_n, ph_bytes, &e->smem_gj_max, &e->cfg);
+    ce = wtg::batch_fp64_prepare();
+    if (ce == cudaSuccess) ce = wtg::batch_fp64_config(max_n, ph_bytes, &e->smem_gj_max, &e->cfg);
   }
+  if (const char* g = getenv("WTG_ENGINE_GRAPHS")) e->use_graphs = atoi(g) != 0;
   if (ce != cudaSuccess) {
     delete e;
     return cuda_fail(ce, "batch config");
@@ -391,6 +419,7 @@ int engine_create(int nmodels, const wtg_model_t* models, int precision, int max
     b.nbot = nbot[i];
     b.top = (const int*)e->lists_d.p + toff[i];
     b.bot = (const int*)e->lists_d.p + boff[i];
+    b.w0 = mixed ? wtg::batch_mixed_w0(m->N) : 0;
     e->model_n.push_back(m->N);
   }
   if (ce == cudaSuccess) ce = e->models_d.ensure(sizeof(wtg::BatchModel) * nmodels);
@@ -412,6 +441,52 @@ int engine_create(int nmodels, const wtg_model_t* models, int precision, int max
                     sizeof(wtg::BatchModel) * nmodels + 64;
   *out = e;
   return WTG_OK;
+}
+
+// one run's stream work for staging capacity C: inputs in, counter reset, the
+// batch kernel, outputs back.  With from_device the kernel reads the point count
+// and the run's scalars from the staged header (a captured graph replays any run
+// of up to C points); otherwise they are kernel arguments (C = the point count).
+cudaError_t engine_enqueue(wtg_engine* e, int C, bool from_device) {
+  const size_t c = (size_t)C;
+  unsigned char* d = (unsigned char*)e->io_d.p;
+  unsigned char* din = d + RUN_HDR;
+  unsigned char* dout = d + e->in_bytes;
+  cudaStream_t s = e->stream;
+  const wtg::BatchRunHeader* hdr = (const wtg::BatchRunHeader*)e->pinned;
+  cudaError_t ce = cudaMemcpyAsync(d, e->pinned, RUN_HDR + 40 * c, cudaMemcpyHostToDevice, s);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(e->counter.p, 0, sizeof(int), s);
+  if (ce != cudaSuccess) return ce;
+  wtg::BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.npts = C;
+  a.run = from_device ? (const wtg::BatchRunHeader*)d : nullptr;
+  a.models = (const wtg::BatchModel*)e->models_d.p;
+  a.pmodel = (const int*)din;
+  a.order = (const int*)(din + 4 * c);
+  a.k = (const double*)(din + 8 * c);
+  a.omega = (const double*)(din + 24 * c);
+  a.eta = (const double*)(din + 32 * c);
+  a.tol = hdr->tol;                      // the direct path: the run's scalars as arguments
+  a.itermax = hdr->itermax;
+  a.divide_by_pi = hdr->divide_by_pi;
+  a.dos_l = (double*)dout;
+  a.dos_r = (double*)(dout + 8 * c);
+  a.dos_bulk = (double*)(dout + 16 * c);
+  a.iters = (int32_t*)(dout + 24 * c);
+  a.status = (uint8_t*)(dout + 28 * c);
+  a.ws = (double2*)e->ws.p;
+  a.ws_stride = e->ws_stride;
+  a.counter = (int*)e->counter.p;
+  a.KC = e->cfg.KC;
+  a.smem_gj_max = e->smem_gj_max;
+  a.wb = e->wb;
+  a.ph_off = e->ph_off;
+  const int grid = std::min(e->grid, C);
+  ce = e->precision == WTG_PREC_MIXED ? wtg::launch_batch_mixed(a, e->cfg, grid, s)
+                                      : wtg::launch_batch_fp64(a, e->cfg, grid, s);
+  if (ce != cudaSuccess) return ce;
+  return cudaMemcpyAsync(e->pinned + e->in_bytes, dout, 29 * c, cudaMemcpyDeviceToHost, s);
 }
 
 int engine_run(wtg_engine* e, int npts, const int* point_model, const double* k,
@@ -439,59 +514,62 @@ int engine_run(wtg_engine* e, int npts, const int* point_model, const double* k,
     order[p] = p;
   }
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
-  // stage inputs: pmodel | order | k (npts x 2) | omega | eta, for npts points
+  // stage inputs in the layout of capacity C: the smallest power of two >= npts
+  // (at least 64, at most max_points) when the run replays a captured graph, npts
+  // otherwise
+  const bool graphed = e->use_graphs;
+  size_t C = (size_t)npts;
+  if (graphed) {
+    C = 64;
+    while (C < (size_t)npts) C <<= 1;
+    C = std::min(C, (size_t)e->max_points);
+  }
   unsigned char* h = e->pinned;
   const size_t n = (size_t)npts;
-  memcpy(h, point_model, 4 * n);
-  memcpy(h + 4 * n, order.data(), 4 * n);
-  memcpy(h + 8 * n, k, 16 * n);
-  memcpy(h + 24 * n, omega, 8 * n);
-  memcpy(h + 32 * n, eta, 8 * n);
-  unsigned char* d = (unsigned char*)e->io_d.p;
+  wtg::BatchRunHeader hdr;
+  memset(&hdr, 0, sizeof(hdr));
+  hdr.npts = npts;
+  hdr.itermax = itermax;
+  hdr.divide_by_pi = divide_by_pi ? 1 : 0;
+  hdr.tol = tol;
+  memcpy(h, &hdr, RUN_HDR);
+  unsigned char* hin = h + RUN_HDR;
+  memcpy(hin, point_model, 4 * n);
+  memcpy(hin + 4 * C, order.data(), 4 * n);
+  memcpy(hin + 8 * C, k, 8 * n);                 // k(:, 1)
+  memcpy(hin + 8 * C + 8 * C, k + n, 8 * n);     // k(:, 2) at column stride C
+  memcpy(hin + 24 * C, omega, 8 * n);
+  memcpy(hin + 32 * C, eta, 8 * n);
+  unsigned char* hout = h + e->in_bytes;
   cudaStream_t s = e->stream;
-  WTG_CK(cudaMemcpyAsync(d, h, 40 * n, cudaMemcpyHostToDevice, s));
-  unsigned char* dout = d + e->in_bytes;
-  WTG_CK(cudaMemsetAsync(e->counter.p, 0, sizeof(int), s));
-  wtg::BatchArgs a;
-  memset(&a, 0, sizeof(a));
-  a.npts = npts;
-  a.models = (const wtg::BatchModel*)e->models_d.p;
-  a.pmodel = (const int*)d;
-  a.order = (const int*)(d + 4 * n);
-  a.k = (const double*)(d + 8 * n);
-  a.omega = (const double*)(d + 24 * n);
-  a.eta = (const double*)(d + 32 * n);
-  a.tol = tol;
-  a.itermax = itermax;
-  a.divide_by_pi = divide_by_pi ? 1 : 0;
-  a.dos_l = (double*)dout;
-  a.dos_r = (double*)(dout + 8 * n);
-  a.dos_bulk = (double*)(dout + 16 * n);
-  a.iters = (int32_t*)(dout + 24 * n);
-  a.status = (uint8_t*)(dout + 28 * n);
-  a.ws = (double2*)e->ws.p;
-  a.ws_stride = e->ws_stride;
-  a.counter = (int*)e->counter.p;
-  a.KC = e->cfg.KC;
-  a.smem_gj_max = e->smem_gj_max;
-  a.wb = e->wb;
-  a.ph_off = e->ph_off;
-  const int grid = std::min(e->grid, npts);
-  if (e->precision == WTG_PREC_MIXED) {
-    WTG_CK(wtg::launch_batch_mixed(a, e->cfg, grid, s));
+  if (graphed) {
+    cudaGraphExec_t ge = nullptr;
+    for (auto& g : e->graphs)
+      if (g.first == (int)C) ge = g.second;
+    if (!ge) {
+      cudaGraph_t graph = nullptr;
+      WTG_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ce = engine_enqueue(e, (int)C, true);
+      const cudaError_t ce2 = cudaStreamEndCapture(s, &graph);
+      if (ce == cudaSuccess) ce = ce2;
+      if (ce == cudaSuccess) ce = cudaGraphInstantiate(&ge, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) return cuda_fail(ce, "engine graph capture");
+      e->graphs.emplace_back((int)C, ge);
+    }
+    WTG_CK(cudaGraphLaunch(ge, s));
+    e->graph_launches += 1;
   } else {
-    WTG_CK(wtg::launch_batch_fp64(a, e->cfg, grid, s));
+    WTG_CK(engine_enqueue(e, (int)C, false));
   }
   e->launches += 1;
-  unsigned char* hout = h + e->in_bytes;
-  WTG_CK(cudaMemcpyAsync(hout, dout, 29 * n, cudaMemcpyDeviceToHost, s));
   WTG_CK(cudaStreamSynchronize(s));
   memcpy(dos_l, hout, 8 * n);
-  memcpy(dos_r, hout + 8 * n, 8 * n);
-  memcpy(dos_bulk, hout + 16 * n, 8 * n);
-  if (iters) memcpy(iters, hout + 24 * n, 4 * n);
-  if (status) memcpy(status, hout + 28 * n, n);
-  return count_flagged(hout + 28 * n, n);
+  memcpy(dos_r, hout + 8 * C, 8 * n);
+  memcpy(dos_bulk, hout + 16 * C, 8 * n);
+  if (iters) memcpy(iters, hout + 24 * C, 4 * n);
+  if (status) memcpy(status, hout + 28 * C, n);
+  return count_flagged(hout + 28 * C, n);
 }
 
 }  // namespace
@@ -970,6 +1048,55 @@ int wtg_engine_create(int nmodels, const wtg_model_t* models, int precision, int
 int wtg_engine_destroy(wtg_engine_t e) {
   if (!e) return fail(WTG_EINVAL, "null engine");
   delete e;
+  return WTG_OK;
+}
+
+int wtg_engine_set_graphs(wtg_engine_t e, int on) {
+  if (!e) return fail(WTG_EINVAL, "null engine");
+  std::lock_guard<std::mutex> lk(e->mu);
+  e->use_graphs = on != 0;
+  return WTG_OK;
+}
+
+int wtg_engine_graph_info(wtg_engine_t e, int* graphs, long long* graph_launches) {
+  if (!e) return fail(WTG_EINVAL, "null engine");
+  std::lock_guard<std::mutex> lk(e->mu);
+  if (graphs) *graphs = (int)e->graphs.size();
+  if (graph_launches) *graph_launches = e->graph_launches;
+  return WTG_OK;
+}
+
+int wtg_tile_set(int precision, int ndim, int value) {
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
+  if (ndim < 1 || ndim > wtg::TILE_MAX_N) return fail(WTG_EINVAL, "ndim outside 1..4096");
+  if (value != 0) {
+    if (precision == WTG_PREC_FP64 && value != 128 && value != 256 && value != 512)
+      return fail(WTG_EINVAL, "FP64 tile: threads per CTA must be 128, 256 or 512");
+    if (precision == WTG_PREC_MIXED &&
+        (value < 8 || (value & 7) != 0 || ndim > wtg::decim_mixed_max_n() ||
+         value > wtg::mixed_w0_max(ndim)))
+      return fail(WTG_EINVAL, "mixed tile: pass width must be a multiple of 8 in 8.." +
+                                  std::to_string(ndim <= wtg::decim_mixed_max_n()
+                                                     ? wtg::mixed_w0_max(ndim) : 0));
+  }
+  wtg::tile_store(precision, ndim, value);
+  return WTG_OK;
+}
+
+int wtg_tile_get(int precision, int ndim, int* value, int* builtin) {
+  if (precision != WTG_PREC_FP64 && precision != WTG_PREC_MIXED)
+    return fail(WTG_EINVAL, "unknown precision mode");
+  if (ndim < 1 || ndim > wtg::TILE_MAX_N) return fail(WTG_EINVAL, "ndim outside 1..4096");
+  int b = 0;
+  if (precision == WTG_PREC_FP64) {
+    b = ndim > wtg::decim_fp64_max_n() ? 256 : wtg::fp64_threads_default(ndim);
+  } else {
+    b = ndim <= wtg::decim_mixed_max_n() ? wtg::mixed_w0_default(ndim) : 0;
+  }
+  const int t = wtg::tile_value(precision, ndim);
+  if (builtin) *builtin = b;
+  if (value) *value = t != 0 ? t : b;
   return WTG_OK;
 }
 

@@ -120,6 +120,7 @@ struct DecimArgs {
   double2* ws;                // [grid][8 or 9][N*N] workspace (decim_fp64_ws_matrices)
   int* counter;               // work counter, zero at launch
   int KC;                     // GEMM k-chunk staged in shared memory
+  int w0;                     // mixed: output-column pass width (tile table; 0 = built-in)
   int ntop, nbot;
   int top[MAX_ORB];           // 1-based orbital lists (TopOrbitals / BottomOrbitals)
   int bot[MAX_ORB];
@@ -135,10 +136,18 @@ struct BatchModel {
   int ntop, nbot;
   const int* top;             // 1-based orbital lists, device
   const int* bot;
+  int w0;                     // mixed: output-column pass width (tile table; 0 = built-in)
+};
+
+// a run's scalars, staged with its points: a captured run reads them from device memory
+struct BatchRunHeader {
+  int npts, itermax, divide_by_pi, pad;
+  double tol, pad2;
 };
 
 struct BatchArgs {
-  int npts;
+  int npts;                   // points, and the column stride of k (a staging capacity in graphs)
+  const BatchRunHeader* run;  // if set, npts / tol / itermax / divide_by_pi are read here
   const BatchModel* models;   // device
   const int* pmodel;          // [npts] model of each point
   const int* order;           // [npts] points in launch order (largest estimated cost first)
@@ -169,7 +178,25 @@ struct DecimConfig {
   size_t smem;                // dynamic shared memory per CTA
   int ctas_per_sm;
   int inv_global = 0;         // FP64: 1 = the inverse runs in global memory (large Ndim)
+  int w0 = 0;                 // mixed: output-column pass width
 };
+
+// Built-in choices and limits of the tunable shapes, and the mixed form's pass
+// width for Ndim N after the tile table.
+int fp64_threads_default(int N);
+int mixed_w0_default(int N);
+int mixed_w0_max(int N);
+int batch_mixed_w0(int N);
+// Raise the batch kernels' dynamic shared-memory limit to the device maximum (once).
+cudaError_t batch_fp64_prepare();
+cudaError_t batch_mixed_prepare();
+
+// Tile table: per-Ndim launch shapes chosen by the autotuner (wtg_tile_set).
+// precision 0 (FP64): threads per CTA of the per-model kernel (128, 256 or 512);
+// precision 1 (mixed): output-column pass width (a multiple of 8).  0 = built-in choice.
+constexpr int TILE_MAX_N = 4096;
+int tile_value(int precision, int N);
+void tile_store(int precision, int N, int value);
 
 // Largest Ndim the shared-memory Gauss-Jordan kernel takes.
 int decim_fp64_max_n();

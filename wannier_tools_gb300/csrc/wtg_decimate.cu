@@ -23,6 +23,8 @@
 // and keeping the pipe fed; pivot searches compare magnitudes as integers.
 #include <algorithm>
 
+#include <mutex>
+
 #include "wtg_common.cuh"
 
 namespace wtg {
@@ -206,10 +208,14 @@ __global__ void __launch_bounds__(256, 1) k_batch_fp64(const __grid_constant__ B
   const int tid = threadIdx.x;
   double2* W = a.ws + (size_t)blockIdx.x * a.ws_stride;
   __shared__ int sinst;
+  const int npts = a.run ? a.run->npts : a.npts;
+  const double tol = a.run ? a.run->tol : a.tol;
+  const int itermax = a.run ? a.run->itermax : a.itermax;
+  const int divide_by_pi = a.run ? a.run->divide_by_pi : a.divide_by_pi;
   for (;;) {
     if (tid == 0) {
       const int q = atomicAdd(a.counter, 1);
-      sinst = q < a.npts ? a.order[q] : -1;
+      sinst = q < npts ? a.order[q] : -1;
     }
     __syncthreads();
     const int p = sinst;
@@ -222,9 +228,9 @@ __global__ void __launch_bounds__(256, 1) k_batch_fp64(const __grid_constant__ B
     fourier_fill(m, a.k[p], a.k[p + a.npts], W, reinterpret_cast<double2*>(smraw + a.ph_off));
     SolveOpts o;
     o.nw = m.nw;
-    o.tol = a.tol;
-    o.itermax = a.itermax;
-    o.divide_by_pi = a.divide_by_pi;
+    o.tol = tol;
+    o.itermax = itermax;
+    o.divide_by_pi = divide_by_pi;
     o.ntop = m.ntop;
     o.nbot = m.nbot;
     o.top = m.top;
@@ -293,6 +299,8 @@ int decim_fp64_max_n() {
 
 int decim_fp64_large_max_n() { return 32 * GJ_ROWS; }
 
+int fp64_threads_default(int N) { return N <= 48 ? 128 : (N <= 80 ? 256 : 512); }
+
 size_t decim_fp64_ws_matrices(const DecimConfig& cfg) { return cfg.inv_global ? 9 : 8; }
 
 cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg, bool force_global) {
@@ -304,7 +312,8 @@ cudaError_t decim_fp64_config(int N, int threads_override, DecimConfig* cfg, boo
   if (e != cudaSuccess) return e;
   const bool gi = force_global || N > decim_fp64_max_n();
   if (gi && N > decim_fp64_large_max_n()) return cudaErrorInvalidValue;
-  int T = threads_override > 0 ? threads_override : (N <= 48 ? 128 : (N <= 80 ? 256 : 512));
+  if (threads_override <= 0) threads_override = tile_value(0, N);
+  int T = threads_override > 0 ? threads_override : fp64_threads_default(N);
   int KC = N;
   if (gi) {
     T = 256;                       // 255 registers: a lane keeps 10 rows of a column
@@ -382,10 +391,27 @@ cudaError_t batch_fp64_config(int max_n, size_t extra_smem, int* smem_gj_max, De
   return cudaSuccess;
 }
 
+// the batch kernel's dynamic shared-memory limit raised once per device to the
+// opt-in maximum (engines of any size launch it, also from captured graphs)
+cudaError_t batch_fp64_prepare() {
+  static std::mutex mu;
+  static bool done[64];
+  int dev = 0, optin = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 64 && done[dev]) return cudaSuccess;
+  cudaFuncAttributes fa;
+  err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, k_batch_fp64);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_batch_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               optin - (int)fa.sharedSizeBytes);
+  if (err == cudaSuccess && dev < 64) done[dev] = true;
+  return err;
+}
+
 cudaError_t launch_batch_fp64(const BatchArgs& a, const DecimConfig& cfg, int grid, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)cfg.smem);
-  if (e != cudaSuccess) return e;
   k_batch_fp64<<<grid, cfg.threads, cfg.smem, s>>>(a);
   return cudaGetLastError();
 }

@@ -39,6 +39,8 @@
 // marks the instance, waits (bounded) for its MMAs and frees tensor memory.
 #include <cuda_bf16.h>
 
+#include <mutex>
+
 #include "wtg_common.cuh"
 
 namespace wtg {
@@ -72,17 +74,27 @@ struct MxPlan {
   int wb;                    // B-plane width of the shared-memory layout (>= w0)
 };
 
-__host__ __device__ inline MxPlan mx_plan(int N) {
+// widest pass: both components side by side, 2 x nacc accumulators of w columns
+// in the 512 tensor-memory columns
+__host__ __device__ inline int mx_wmax(int N) { return (512 / (2 * (N > 256 ? 6 : 5))) & ~7; }
+
+// w0_req: a pass width from the tile table (a multiple of 8 in [8, mx_wmax]); any
+// other value takes the built-in choice (the fewest passes, evenly split)
+__host__ __device__ inline MxPlan mx_plan(int N, int w0_req = 0) {
   MxPlan p;
   p.N = N;
   p.NP = (N + 15) & ~15;
   p.nrb = (N + 127) / 128;
   p.nacc = N > 256 ? 6 : 5;
-  // both components side by side in one pass: 2 x nacc accumulators of w columns
-  const int wmax = (512 / (2 * p.nacc)) & ~7;
-  p.ncb = (p.NP + wmax - 1) / wmax;
-  p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 7) & ~7;
-  while (p.ncb > 1 && (p.ncb - 1) * p.w0 >= p.NP) --p.ncb;
+  const int wmax = mx_wmax(N);
+  if (w0_req >= 8 && w0_req <= wmax && (w0_req & 7) == 0) {
+    p.w0 = w0_req;
+    p.ncb = (p.NP + w0_req - 1) / w0_req;
+  } else {
+    p.ncb = (p.NP + wmax - 1) / wmax;
+    p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 7) & ~7;
+    while (p.ncb > 1 && (p.ncb - 1) * p.w0 >= p.NP) --p.ncb;
+  }
   p.wb = p.w0;
   return p;
 }
@@ -1226,7 +1238,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const __grid_constan
                                                             int ns_iter, int ns_final) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
-  const MxPlan pl = mx_plan(N);
+  const MxPlan pl = mx_plan(N, a.w0);
   MxShared s = mx_layout(smraw, pl.wb);
   MxState st;
   mx_setup(s, st);
@@ -1292,10 +1304,14 @@ __global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__
   MxState st;
   mx_setup(s, st);
   double2* W = a.ws + (size_t)blockIdx.x * a.ws_stride;
+  const int npts = a.run ? a.run->npts : a.npts;
+  const double tol = a.run ? a.run->tol : a.tol;
+  const int itermax = a.run ? a.run->itermax : a.itermax;
+  const int divide_by_pi = a.run ? a.run->divide_by_pi : a.divide_by_pi;
   for (;;) {
     if (tid == 0) {
       const int q = atomicAdd(a.counter, 1);
-      s.misc[0] = q < a.npts ? a.order[q] : -1;
+      s.misc[0] = q < npts ? a.order[q] : -1;
     }
     __syncthreads();
     const int p = s.misc[0];
@@ -1306,14 +1322,14 @@ __global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__
       continue;
     }
     const BatchModel& m = a.models[a.pmodel[p]];
-    MxPlan pl = mx_plan(m.N);
+    MxPlan pl = mx_plan(m.N, m.w0);
     pl.wb = a.wb;
     fourier_fill(m, a.k[p], a.k[p + a.npts], W, reinterpret_cast<double2*>(smraw + a.ph_off));
     MxOpts o;
     o.nw = m.nw;
-    o.tol = a.tol;
-    o.itermax = a.itermax;
-    o.divide_by_pi = a.divide_by_pi;
+    o.tol = tol;
+    o.itermax = itermax;
+    o.divide_by_pi = divide_by_pi;
     o.ntop = m.ntop;
     o.nbot = m.nbot;
     o.top = m.top;
@@ -1362,7 +1378,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
   mx_teardown(s, st);
 }
 
-size_t mixed_smem(int N, int wb = 0) {
+size_t mixed_smem(int N, int wb = 0) {     // wb = 0: the built-in plan's width
   const MxPlan pl = mx_plan(N);
   const size_t bufbytes = (size_t)bufbytes_of(wb > 0 ? wb : pl.w0);
   // the FP32 Gauss-Jordan matrix ((N+1)*N float2, Ndim <= MX_SMEM_GJ_N) or the
@@ -1384,8 +1400,10 @@ cudaError_t decim_mixed_config(int N, DecimConfig* cfg) {
   cfg->threads = MX_T;
   cfg->KC = 0;
   cfg->RP = 0;
+  cfg->w0 = mx_plan(N, tile_value(1, N)).w0;
   // at least 116 KB so that two CTAs never share an SM (each allocates all 512 TMEM columns)
-  cfg->smem = mixed_smem(N) > (size_t)(116 << 10) ? mixed_smem(N) : (size_t)(116 << 10);
+  const size_t sm = mixed_smem(N, cfg->w0);
+  cfg->smem = sm > (size_t)(116 << 10) ? sm : (size_t)(116 << 10);
   cudaError_t e = cudaFuncSetAttribute(k_decimate_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)cfg->smem);
   if (e != cudaSuccess) return e;
@@ -1406,7 +1424,10 @@ cudaError_t batch_mixed_config(int max_n, int* wb, DecimConfig* cfg) {
   if (max_n > MX_MAXN) return cudaErrorInvalidValue;
   int w = 16;
   size_t smem = 0;
-  for (int n = 1; n <= max_n; ++n) w = w > mx_plan(n).w0 ? w : mx_plan(n).w0;
+  for (int n = 1; n <= max_n; ++n) {
+    const int wn = mx_plan(n, tile_value(1, n)).w0;
+    w = w > wn ? w : wn;
+  }
   for (int n = 1; n <= max_n; ++n) {
     const size_t t = mixed_smem(n, w);
     smem = smem > t ? smem : t;
@@ -1421,14 +1442,36 @@ cudaError_t batch_mixed_config(int max_n, int* wb, DecimConfig* cfg) {
   return cudaSuccess;
 }
 
+// as batch_fp64_prepare
+cudaError_t batch_mixed_prepare() {
+  static std::mutex mu;
+  static bool done[64];
+  int dev = 0, optin = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 64 && done[dev]) return cudaSuccess;
+  cudaFuncAttributes fa;
+  err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, k_batch_mixed);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_batch_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               optin - (int)fa.sharedSizeBytes);
+  if (err == cudaSuccess && dev < 64) done[dev] = true;
+  return err;
+}
+
 cudaError_t launch_batch_mixed(const BatchArgs& a, const DecimConfig& cfg, int grid,
                                cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)cfg.smem);
-  if (e != cudaSuccess) return e;
   k_batch_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 6, 8);
   return cudaGetLastError();
 }
+
+int batch_mixed_w0(int N) { return mx_plan(N, tile_value(1, N)).w0; }
+
+int mixed_w0_default(int N) { return mx_plan(N).w0; }
+
+int mixed_w0_max(int N) { return mx_wmax(N); }
 
 cudaError_t launch_mixed_unit(int op, int N, const double2* X, const double2* Y, double2* C,
                               double2* ws, int ns, int* status, cudaStream_t s) {
