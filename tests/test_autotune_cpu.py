@@ -19,6 +19,13 @@ def test_candidates():
         autotune.candidates("tf32", 40)
 
 
+def test_sample_grows_at_small_ndim():
+    assert autotune.default_solves(152, 112) == 304
+    assert autotune.default_solves(152, 264) == 304
+    assert autotune.default_solves(152, 40) == round(304 * (112 / 40) ** 3)
+    assert autotune.default_solves(152, 8) == 16384
+
+
 def test_device_key_drops_memory():
     info = "NVIDIA GB300, 152 SMs, cc 10.3, 275.0 GiB"
     assert autotune.device_key(info) == "NVIDIA GB300, 152 SMs, cc 10.3"

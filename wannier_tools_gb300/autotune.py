@@ -65,6 +65,13 @@ def shape_for(nw_np: tuple[int, int] | None, ndim: int) -> tuple[int, int]:
     return ndim, 1
 
 
+def default_solves(nsm: int, ndim: int) -> int:
+    """Solves per timed call: many waves at small Ndim, where several CTAs share an
+    SM and a two-wave sample hides the occupancy a shape gives (about the work of
+    two waves at Ndim 112, at least 2 per SM, at most 16384)."""
+    return int(min(16384, max(2 * nsm, round(2 * nsm * (112.0 / ndim) ** 3))))
+
+
 def _time_candidate(api, model, form, ndim, value, kpts, omegas, eta, top, bot, reps):
     prec = FORMS[form]
     before = api.get_tile(prec, ndim)[0]
@@ -88,10 +95,10 @@ def tune(ndims, forms=("fp64", "mixed"), reps: int = 3, solves: int | None = Non
     from ._lib import load
     load()
     nsm = int(device_key(api.device_info()).split(", ")[1].split()[0])
-    nsolves = solves or 2 * nsm
     entries: dict = {f: {} for f in forms}
     timings: dict = {f: {} for f in forms}
     for ndim in ndims:
+        nsolves = solves or default_solves(nsm, ndim)
         nw, np_ = shape_for(None, ndim)
         sm = synthetic.make_model(nw, np_, seed=seed + ndim)
         kpts = synthetic.random_kpoints(2, seed=seed)
@@ -120,7 +127,7 @@ def tune(ndims, forms=("fp64", "mixed"), reps: int = 3, solves: int | None = Non
                 timings[form][str(ndim)] = {str(v): round(t * 1e3, 3) for v, t in times.items()}
                 log(f"{form} Ndim {ndim}: " + ", ".join(f"{v}: {t * 1e3:.2f} ms" for v, t in times.items())
                     + f" -> {best}")
-    return {"entries": entries, "ms": timings, "solves": nsolves, "reps": reps}
+    return {"entries": entries, "ms": timings, "reps": reps}
 
 
 def save(result: dict, device: str, path: Path = TABLE) -> None:

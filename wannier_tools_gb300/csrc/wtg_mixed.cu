@@ -500,17 +500,20 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int
   }
 }
 
-// C = X * Y through the epilogue; returns this thread's FP32 partial of sum |C|
-// (OZ_STORE_NORM, OZ_IMINUS).  out0/out1/src: FP64 N x N column-major.
+// C = X * Y through the epilogue; returns this thread's partial of sum |C|:
+// OZ_STORE_NORM (the decimation's convergence norm) sums each |C_ij| (to FP32
+// precision) in FP64; OZ_IMINUS (the refinement residual) sums in FP32.
+// out0/out1/src: FP64 N x N column-major.
 template <int EPI>
-__device__ float oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y,
-                         const MxPlan& pl, double2* out0, double2* out1, const double2* src,
-                         MxShared& s, MxState& st) {
+__device__ double oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y,
+                          const MxPlan& pl, double2* out0, double2* out1, const double2* src,
+                          MxShared& s, MxState& st) {
   const int N = pl.N, tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
   const int nacc = pl.nacc, WB = pl.wb;
   const int npass = pl.ncb;
   float nrm = 0.f;
+  double nrm_d = 0.0;
   oz_exponents(X, Y, N, s);
   __syncthreads();
   for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
@@ -616,7 +619,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
                     const float hi = fmaxf(re, im), lo = fminf(re, im);
                     if (hi > 0.f) {
                       const float r = lo / hi;
-                      nrm += hi * sqrtf(fmaf(r, r, 1.f));
+                      nrm_d += (double)(hi * sqrtf(fmaf(r, r, 1.f)));
                     }
                   }
                 } else if (EPI == OZ_IMINUS) {
@@ -637,7 +640,7 @@ __device__ float oz_gemm(const double2* __restrict__ X, const double2* __restric
       tc_fence_after();
     }
   }
-  return nrm;
+  return EPI == OZ_STORE_NORM ? nrm_d : (double)nrm;
 }
 
 __device__ float block_sum_f(float v, MxShared& s) {
@@ -653,6 +656,26 @@ __device__ float block_sum_f(float v, MxShared& s) {
   }
   __syncthreads();
   t = s.red[0];
+  __syncthreads();
+  return t;
+}
+
+// block sum in FP64 (16 warps: the 32-float reduction area holds 16 doubles)
+static_assert(MX_T / 32 <= 16, "block_sum_d keeps one double per warp in s.red");
+__device__ double block_sum_d(double v, MxShared& s) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double* red = reinterpret_cast<double*>(s.red);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) t += red[w];
+    red[0] = t;
+  }
+  __syncthreads();
+  t = red[0];
   __syncthreads();
   return t;
 }
@@ -1090,7 +1113,7 @@ __device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int 
                                      : gj32_global<MX_ROWS>(X, w, N, Mi, *Gp, Wf, s);
   float prev = 3.0e38f;
   for (int t = 0; t < ns_max && !st.abort; ++t) {
-    const float part = oz_gemm<OZ_IMINUS>(Mi, *Gp, pl, R, nullptr, nullptr, s, st);  // R = I - M G
+    const float part = (float)oz_gemm<OZ_IMINUS>(Mi, *Gp, pl, R, nullptr, nullptr, s, st);  // R = I - M G
     const float res = block_sum_f(part, s);
     if (!(res < 0.25f * prev)) break;                 // no longer converging (or NaN)
     oz_gemm<OZ_ADDTO>(*Gp, R, pl, *Gnp, nullptr, *Gp, s, st);                         // Gn = G + G R
@@ -1170,7 +1193,7 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st);
     oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);
     oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st);
-    const float part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st);
+    const double part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st);
     oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st);
     double2* t0 = Al;
     Al = Gn;
@@ -1178,8 +1201,8 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     double2* t1 = Be;
     Be = R;
     R = t1;
-    const float nrm = block_sum_f(part, s);
-    if ((double)nrm <= o.tol) {
+    const double nrm = block_sum_d(part, s);     // :120-122, summed and tested in FP64
+    if (nrm <= o.tol) {
       conv = true;
       break;
     }
