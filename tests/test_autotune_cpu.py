@@ -26,6 +26,13 @@ def test_sample_grows_at_small_ndim():
     assert autotune.default_solves(152, 8) == 16384
 
 
+def test_model_shape_per_ndim():
+    assert autotune.shape_for(112) == (56, 2)
+    assert autotune.shape_for(264) == (132, 2)
+    assert autotune.shape_for(39) == (13, 3)
+    assert autotune.shape_for(7) == (7, 1)
+
+
 def test_device_key_drops_memory():
     info = "NVIDIA GB300, 152 SMs, cc 10.3, 275.0 GiB"
     assert autotune.device_key(info) == "NVIDIA GB300, 152 SMs, cc 10.3"

@@ -55,10 +55,8 @@ def device_key(info: str) -> str:
     return ", ".join(info.split(", ")[:3])
 
 
-def shape_for(nw_np: tuple[int, int] | None, ndim: int) -> tuple[int, int]:
+def shape_for(ndim: int) -> tuple[int, int]:
     """(Num_wann, Np) of the synthetic model used for an Ndim."""
-    if nw_np is not None:
-        return nw_np
     for np_ in (2, 3, 1):
         if ndim % np_ == 0 and ndim // np_ >= 2:
             return ndim // np_, np_
@@ -99,7 +97,7 @@ def tune(ndims, forms=("fp64", "mixed"), reps: int = 3, solves: int | None = Non
     timings: dict = {f: {} for f in forms}
     for ndim in ndims:
         nsolves = solves or default_solves(nsm, ndim)
-        nw, np_ = shape_for(None, ndim)
+        nw, np_ = shape_for(ndim)
         sm = synthetic.make_model(nw, np_, seed=seed + ndim)
         kpts = synthetic.random_kpoints(2, seed=seed)
         omegas = np.linspace(-0.5, 0.5, max(1, nsolves // 2)) / 27.211385
