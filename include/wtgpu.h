@@ -323,8 +323,8 @@ int wtg_engine_run(wtg_engine_t engine, int npts, const int* point_model, const 
                    int divide_by_pi, double* dos_l, double* dos_r, double* dos_bulk, int* iters,
                    unsigned char* status);
 /*
- * CUDA graphs (on by default; WTG_ENGINE_GRAPHS=0 in the environment turns them
- * off for new engines): a run's copy-in, counter reset, batch kernel and
+ * CUDA graphs (on by default; wtg_engine_set_graphs(engine, 0) turns them off
+ * for that engine): a run's copy-in, counter reset, batch kernel and
  * copy-out are captured once per staging capacity (the powers of two from 64 up
  * to max_points) and replayed with one cudaGraphLaunch; the point count and the
  * run's scalars travel in the staged header.  Results are bit-identical with
@@ -355,6 +355,29 @@ int wtg_batch_spectrum(int nmodels, const wtg_model_t* models, int npts, const i
                        int itermax, const int* ntop, const int* top, const int* nbot,
                        const int* bot, int divide_by_pi, int precision, double* dos_l,
                        double* dos_r, double* dos_bulk, int* iters, unsigned char* status);
+
+/*
+ * Test-only switches, process-wide (no counterpart in the reference).  They
+ * exist so that a test can reach code paths that normal inputs do not; a
+ * production caller never sets them.  value 0 restores normal operation.
+ *   WTG_TEST_FP64_GLOBAL_INVERSE  non-zero: the per-model FP64 kernel inverts in
+ *                                 global memory at every Ndim (the variant that
+ *                                 normally runs above Ndim 119; both agree bit
+ *                                 for bit)
+ *   WTG_TEST_MIXED_SPIN_LIMIT     > 0: the mixed kernels' pipeline waits on the
+ *                                 tensor cores give up after this many
+ *                                 non-blocking polls instead of the built-in
+ *                                 bound, so that a test can make them run out:
+ *                                 the points get WTG_PT_TIMEOUT and the call
+ *                                 returns normally.  Read when a launch is
+ *                                 made (an engine's captured graphs keep the
+ *                                 value they were captured with).
+ * Returns WTG_OK, or WTG_EINVAL for an unknown option or a negative value.
+ */
+#define WTG_TEST_FP64_GLOBAL_INVERSE 1
+#define WTG_TEST_MIXED_SPIN_LIMIT    2
+#define WTG_TEST_OPTIONS             3
+int wtg_test_option(int option, int value);
 
 #ifdef __cplusplus
 }

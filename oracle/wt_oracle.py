@@ -136,11 +136,36 @@ def mat_mul(a, b):
     return blas.zgemm(1.0, a, b)
 
 
-def surfgreen_1985(omega, h00, h01, eta, accuracy=ACCURACY_REF, itermax=ITERMAX_REF):
+# The same two operations in another valid FP64 rounding order, used only to
+# measure how far two correct FP64 evaluations of the reference's algorithm
+# can lie apart at a point (its FP64 noise floor): the inverse by zgetrf +
+# zgetri instead of zgesv with an identity right-hand side, and each product
+# with its K sum split in two halves that are added.  Neither is "more
+# correct"; a system LAPACK/BLAS other than scipy's (the reference links
+# whatever it was built with, src/Makefile:42) differs from the oracle in the
+# same way.
+def inv_reordered(a):
+    lu, piv, info = lapack.zgetrf(np.asfortranarray(a))
+    if info != 0:
+        return np.eye(a.shape[0], dtype=np.complex128), int(info)
+    x, info2 = lapack.zgetri(lu, piv)
+    return x, int(info2)
+
+
+def mat_mul_reordered(a, b):
+    h = a.shape[1] // 2
+    return blas.zgemm(1.0, a[:, :h], b[:h]) + blas.zgemm(1.0, a[:, h:], b[h:])
+
+
+def surfgreen_1985(omega, h00, h01, eta, accuracy=ACCURACY_REF, itermax=ITERMAX_REF,
+                   reordered=False):
     """Lopez-Sancho (1985) decimation, src/surfgreen.f90:7-137.
 
     Returns (GLL, GRR, GB, iters, status): iters = iterations executed
-    (1..itermax), status a bitmask of ST_* flags."""
+    (1..itermax), status a bitmask of ST_* flags.  reordered=True evaluates
+    the same steps with inv_reordered / mat_mul_reordered (noise-floor probe)."""
+    inv_ = inv_reordered if reordered else inv
+    mat_mul_ = mat_mul_reordered if reordered else mat_mul
     n = h00.shape[0]
     ones = np.asfortranarray(np.eye(n, dtype=np.complex128))
     epsiloni = np.asfortranarray(h00.copy())              # :74-78
@@ -154,20 +179,20 @@ def surfgreen_1985(omega, h00, h01, eta, accuracy=ACCURACY_REF, itermax=ITERMAX_
     converged = False
     for it in range(1, itermax + 1):                      # :86
         iters = it
-        g0, info = inv(omegac * ones - epsiloni)           # :88-89
+        g0, info = inv_(omegac * ones - epsiloni)          # :88-89
         if info != 0:
             status |= ST_SINGULAR
-        mat1 = mat_mul(alphai, g0)                         # :92
-        mat2 = mat_mul(betai, g0)                          # :95
-        g0 = mat_mul(mat1, betai)                          # :98
+        mat1 = mat_mul_(alphai, g0)                        # :92
+        mat2 = mat_mul_(betai, g0)                         # :95
+        g0 = mat_mul_(mat1, betai)                         # :98
         epsiloni = epsiloni + g0                           # :99
         epsilons = epsilons + g0                           # :102
-        g0 = mat_mul(mat2, alphai)                         # :107
+        g0 = mat_mul_(mat2, alphai)                        # :107
         epsiloni = epsiloni + g0                           # :108
         epsilons_t = epsilons_t + g0                       # :110
-        g0 = mat_mul(mat1, alphai)                         # :113
+        g0 = mat_mul_(mat1, alphai)                        # :113
         alphai = g0
-        g0 = mat_mul(mat2, betai)                          # :116
+        g0 = mat_mul_(mat2, betai)                         # :116
         betai = g0
         real_temp = float(np.sum(np.abs(alphai)))          # :120
         if real_temp <= accuracy:                          # :121
@@ -175,13 +200,13 @@ def surfgreen_1985(omega, h00, h01, eta, accuracy=ACCURACY_REF, itermax=ITERMAX_
             break
     if not converged:
         status |= ST_NOT_CONVERGED
-    gll, info = inv(omegac * ones - epsilons)              # :127-128
+    gll, info = inv_(omegac * ones - epsilons)             # :127-128
     if info != 0:
         status |= ST_SINGULAR
-    grr, info = inv(omegac * ones - epsilons_t)            # :130-131
+    grr, info = inv_(omegac * ones - epsilons_t)           # :130-131
     if info != 0:
         status |= ST_SINGULAR
-    gb, info = inv(omegac * ones - epsiloni)               # :133-134
+    gb, info = inv_(omegac * ones - epsiloni)              # :133-134
     if info != 0:
         status |= ST_SINGULAR
     return gll, grr, gb, iters, status
@@ -294,12 +319,13 @@ def kplane_grid(nk1, nk2, k2d_start, vec1, vec2):
 
 def surface_spectrum(hmnr, irvec, ndegen, nw, np_, kpts, omegas, eta, top, bot,
                      scale=1.0, accuracy=ACCURACY_REF, itermax=ITERMAX_REF,
-                     ijmax=IJMAX_REF, with_spin=False, loto=None):
+                     ijmax=IJMAX_REF, with_spin=False, loto=None, reordered=False):
     """Loop body of surfstat (src/surfstat.f90:123-197) / SurfaceDOSkk
     (src/fermiarc.f90:206-248) over an explicit (k, omega) list.
 
     Returns a dict of (nk, nomega) arrays: dos_l, dos_r, dos_bulk, iters,
-    status (and sx_l..sz_r when with_spin)."""
+    status (and sx_l..sz_r when with_spin).  reordered=True: the decimation in
+    the other FP64 rounding order (surfgreen_1985's noise-floor probe)."""
     nk = len(kpts)
     nwo = len(omegas)
     out = {name: np.zeros((nk, nwo)) for name in ("dos_l", "dos_r", "dos_bulk")}
@@ -314,7 +340,8 @@ def surface_spectrum(hmnr, irvec, ndegen, nw, np_, kpts, omegas, eta, top, bot,
         else:
             h00, h01 = ham_qlayer2qlayer_loto(kpts[ik], hmnr, irvec, ndegen, nw, np_, *loto, ijmax=ijmax)
         for j in range(nwo):
-            gll, grr, gb, it, st = surfgreen_1985(omegas[j], h00, h01, eta, accuracy, itermax)
+            gll, grr, gb, it, st = surfgreen_1985(omegas[j], h00, h01, eta, accuracy, itermax,
+                                                  reordered=reordered)
             dl, dr, db = spectral_sums(gll, grr, gb, top, bot, nw, scale)
             out["dos_l"][ik, j] = dl
             out["dos_r"][ik, j] = dr

@@ -1,9 +1,9 @@
 """Generate the committed fixtures under tests/golden/.
 
-Run from the repository root in an environment that has the reference
-checkout (it reads examples/3DWeyl-model/Weyl3D_hr.dat from it):
+Run from the repository root with the path of a reference checkout (it
+reads examples/3DWeyl-model/Weyl3D_hr.dat from it):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the wannier_tools checkout>
 
 Fixtures:
   weyl3d_hr_model.npz    the reference's 2-band Weyl model (examples/3DWeyl-model/
@@ -78,4 +78,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the wannier_tools checkout>")
+    main(sys.argv[1])

@@ -5,13 +5,11 @@ The panel variant applies the same operations in the same order as the
 shared-memory Gauss-Jordan, so at Ndim <= 119, forced onto the panel variant,
 it must reproduce the shared-memory kernel bit for bit; above 119 it is checked
 against the oracle at the 1e-9 relative bound of the plain form."""
-import os
-
 import numpy as np
 import pytest
 
 from oracle import wt_oracle as O
-from wannier_tools_gb300 import api, synthetic
+from wannier_tools_gb300 import _lib, api, synthetic
 from wannier_tools_gb300._lib import PREC_FP64
 
 pytestmark = pytest.mark.gpu
@@ -29,18 +27,16 @@ def nrel(a, b):
 
 
 def _spectrum(m, kp, om, eta, top, bot, spin=False, force_global=False):
-    old = os.environ.get("WTG_FP64_GLOBAL_INVERSE")
-    os.environ["WTG_FP64_GLOBAL_INVERSE"] = "1" if force_global else "0"
+    # the test-only switch that makes the FP64 kernel invert in global memory at any Ndim
+    lib = _lib.load()
+    assert lib.wtg_test_option(_lib.TEST_FP64_GLOBAL_INVERSE, 1 if force_global else 0) == 0
     try:
         with api.Model.from_surface_model(m) as g:
             if spin:
                 return g.surface_spectrum_spin(kp, om, eta, top, bot, arc=True)
             return g.surface_spectrum(kp, om, eta, top, bot)
     finally:
-        if old is None:
-            del os.environ["WTG_FP64_GLOBAL_INVERSE"]
-        else:
-            os.environ["WTG_FP64_GLOBAL_INVERSE"] = old
+        lib.wtg_test_option(_lib.TEST_FP64_GLOBAL_INVERSE, 0)
 
 
 @pytest.mark.parametrize("nw,np_", [(3, 1), (20, 2), (13, 3), (56, 2)])

@@ -68,7 +68,9 @@ def test_noalloc_matches_allocating_entry_point(built_lib):
 
 
 def test_noalloc_scratch_caps_the_grid_ndim_112(built_lib):
-    # 8 x 112^2 complex per CTA: the fixed scratch holds 40 CTAs, fewer than the GPU's 152
+    # 8 x 112^2 complex per CTA: the fixed scratch holds (64 MiB - 256 B) // (16 * 8 * 112^2) = 41
+    # CTAs, fewer than the GPU's 152
+    assert ((64 << 20) - 256) // (16 * 8 * 112 * 112) == 41
     _run_case(built_lib, 56, 2, 50, [0.0], 1e-3, list(range(1, 57)), list(range(1, 57)), seed=7)
 
 

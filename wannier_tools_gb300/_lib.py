@@ -11,10 +11,8 @@ import os
 import warnings
 from pathlib import Path
 
-# the in-tree build; WTG_LIBRARY names another build of the same library (an
-# experimental or instrumented build) to load instead
-LIB_PATH = Path(os.environ["WTG_LIBRARY"]) if os.environ.get("WTG_LIBRARY") else \
-    Path(__file__).resolve().parent / "libwtgpu.so"
+# the in-tree build (the only library this package loads)
+LIB_PATH = Path(__file__).resolve().parent / "libwtgpu.so"
 
 WTG_OK = 0
 WTG_EINVAL = -1
@@ -30,6 +28,10 @@ PT_TIMEOUT = 8
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+
+# test-only switches of wtg_test_option
+TEST_FP64_GLOBAL_INVERSE = 1
+TEST_MIXED_SPIN_LIMIT = 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -78,6 +80,7 @@ SIGNATURES = {
                                       _i32p, _u8p]),
     "wtg_jdos_kpath": (C.c_int, [C.c_int, C.c_int, _dp, _dp]),
     "wtg_jdos_kplane": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp]),
+    "wtg_test_option": (C.c_int, [C.c_int, C.c_int]),
     "wtg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "wtg_device_info": (C.c_int, [C.c_char_p, C.c_int]),
 }
@@ -91,12 +94,12 @@ class WtgError(RuntimeError):
         self.code = code
 
 
-def load(path: Path | None = None) -> C.CDLL:
-    """Load the library (building it first only when asked by the caller)."""
+def load() -> C.CDLL:
+    """Load the in-tree library (building it is the caller's step)."""
     global _lib
     if _lib is not None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = LIB_PATH
     if not p.exists():
         raise RuntimeError(f"{p} is not built; call wannier_tools_gb300.build() first "
                            "(there is no CPU fallback for this path)")

@@ -17,6 +17,7 @@
 
 #include "../../include/wtgpu.h"
 #include "wtg_common.cuh"
+#include "wtg_plan.h"
 
 namespace {
 
@@ -65,6 +66,18 @@ constexpr size_t H_CHUNK_BYTES = (size_t)8 << 30;
 
 namespace wtg {
 void set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
+namespace {
+std::atomic<int> g_test_opts[WTG_TEST_OPTIONS];
+}  // namespace
+
+int test_option(int option) {
+  return option >= 0 && option < WTG_TEST_OPTIONS ? g_test_opts[option].load() : 0;
+}
+
+void set_test_option(int option, int value) {
+  if (option >= 0 && option < WTG_TEST_OPTIONS) g_test_opts[option].store(value);
+}
 }  // namespace wtg
 
 struct wtg_model {
@@ -126,13 +139,12 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
                                       (mixed ? "mixed" : "FP64") + " kernel limit " +
                                       std::to_string(nmax));
   wtg::DecimConfig cfg;
-  int thr = 0;
-  if (const char* env = getenv("WTG_DECIM_THREADS")) thr = atoi(env);
   if (mixed) {
     WTG_CK(wtg::decim_mixed_config(N, &cfg));
   } else {
-    const char* gi = getenv("WTG_FP64_GLOBAL_INVERSE");   // testing: force the large-Ndim variant
-    WTG_CK(wtg::decim_fp64_config(N, thr, &cfg, gi && atoi(gi) != 0));
+    // the large-Ndim (global-memory inverse) variant at any Ndim when a test asks for it
+    WTG_CK(wtg::decim_fp64_config(N, 0, &cfg,
+                                  wtg::test_option(WTG_TEST_FP64_GLOBAL_INVERSE) != 0));
   }
   const size_t ws_mats = mixed ? wtg::decim_mixed_ws_matrices() : wtg::decim_fp64_ws_matrices(cfg);
   if (cfg.ctas_per_sm < 1) return fail(WTG_EUNSUPPORTED, "decimation kernel does not fit an SM");
@@ -140,10 +152,12 @@ int run_spectrum(wtg_model* m, int nk, const double* d_k, int nomega, const doub
   WTG_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, m->device));
 
   const size_t hk = sizeof(double2) * 2 * (size_t)N * N;   // H00+H01 per k
-  int kchunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nk, H_CHUNK_BYTES / hk));
-  kchunk = std::min(kchunk, 65535 * 8);
-  const long long max_inst = (long long)kchunk * nomega;
   const int grid_max = cfg.ctas_per_sm * nsm;
+  const int kchunk = wtg::spectrum_kchunk(nk, nomega, N, grid_max, H_CHUNK_BYTES);
+  if (kchunk < 1)
+    return fail(WTG_EINVAL, "nomega " + std::to_string(nomega) + " exceeds " +
+                                std::to_string(INT_MAX - grid_max) + " (instances are 32-bit)");
+  const long long max_inst = (long long)kchunk * nomega;
   const int grid = (int)std::min<long long>(grid_max, max_inst);
 
   WTG_CK(m->phase.ensure(sizeof(double2) * (size_t)kchunk * std::max(1, m->nRu)));
@@ -370,7 +384,6 @@ int engine_create(int nmodels, const wtg_model_t* models, int precision, int max
     ce = wtg::batch_fp64_prepare();
     if (ce == cudaSuccess) ce = wtg::batch_fp64_config(max_n, ph_bytes, &e->smem_gj_max, &e->cfg);
   }
-  if (const char* g = getenv("WTG_ENGINE_GRAPHS")) e->use_graphs = atoi(g) != 0;
   if (ce != cudaSuccess) {
     delete e;
     return cuda_fail(ce, "batch config");
@@ -1020,6 +1033,13 @@ int wtg_surface_spectrum_spin(wtg_model_t m, int nk, const double* k, int nomega
     WTG_CK(cudaMemcpyAsync(iters, m->out_it.p, sizeof(int32_t) * npts, cudaMemcpyDeviceToHost, s));
   WTG_CK(cudaStreamSynchronize(s));
   return count_flagged(st_host, npts);
+}
+
+int wtg_test_option(int option, int value) {
+  if (option < 1 || option >= WTG_TEST_OPTIONS) return fail(WTG_EINVAL, "unknown test option");
+  if (value < 0) return fail(WTG_EINVAL, "test option value < 0");
+  wtg::set_test_option(option, value);
+  return WTG_OK;
 }
 
 int wtg_last_error(char* buf, int len) {

@@ -241,4 +241,8 @@ cudaError_t launch_fp64_unit(int op, int N, const double2* X, const double2* Y, 
 // Sets the calling thread's message returned by wtg_last_error.
 void set_last_error(const char* msg);
 
+// Process-wide test switches (wtg_test_option; WTG_TEST_* of include/wtgpu.h); 0 = off.
+int test_option(int option);
+void set_test_option(int option, int value);
+
 }  // namespace wtg

@@ -41,6 +41,7 @@
 
 #include <mutex>
 
+#include "../../include/wtgpu.h"
 #include "wtg_common.cuh"
 
 namespace wtg {
@@ -129,12 +130,29 @@ __device__ __forceinline__ void mma_commit(uint64_t* mb) {
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* mb, uint32_t parity) {
+// Bounded wait for an mbarrier phase.  limit 0: up to SPIN_LIMIT blocking
+// try_wait polls (the normal bound); limit > 0 (a test's bound): that many
+// non-blocking test_wait polls, so that a short limit reliably runs out while
+// the tensor cores are still busy.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mb, uint32_t parity, unsigned limit = 0) {
   const uint32_t a = saddr(mb);
-  for (unsigned spin = 0; spin < SPIN_LIMIT; ++spin) {
+  if (limit == 0) {
+    for (unsigned spin = 0; spin < SPIN_LIMIT; ++spin) {
+      uint32_t ok;
+      asm volatile(
+          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+          " selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(ok)
+          : "r"(a), "r"(parity)
+          : "memory");
+      if (ok) return true;
+    }
+    return false;
+  }
+  for (unsigned spin = 0; spin < limit; ++spin) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
         : "r"(a), "r"(parity)
@@ -285,11 +303,15 @@ struct MxState {           // per-thread copies of the (uniform) pipeline counte
   uint32_t ncommit[2];
   uint32_t nwaited[2];
   int abort;
+  unsigned spin;           // pipeline waits' bound (0 = built-in; see mbar_wait)
 };
 
 __device__ __forceinline__ void buffer_ready(MxShared& s, MxState& st, int b) {
   if (st.ncommit[b] > st.nwaited[b]) {
-    if (!mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1)) st.abort = 1;
+    if (!mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1, st.spin)) {
+      st.abort = 1;        // the buffer's MMAs stay pending: only the teardown waits for them
+      return;
+    }
     st.nwaited[b] = st.ncommit[b];
   }
 }
@@ -527,7 +549,8 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
         const int b = c & 1;
         if (tid >= 32) {     // warps 1.. generate while warp 0 issues the previous chunk
           buffer_ready(s, st, b);
-          oz_generate(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32);
+          if (!st.abort)
+            oz_generate(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
@@ -543,7 +566,7 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
       }
       // all MMAs of this pass: the last commit covers every earlier one
       const int bl = (nch - 1) & 1;
-      if (!st.abort && !mbar_wait(&s.mbar[bl], (st.ncommit[bl] - 1) & 1)) st.abort = 1;
+      if (!st.abort && !mbar_wait(&s.mbar[bl], (st.ncommit[bl] - 1) & 1, st.spin)) st.abort = 1;
       if (!st.abort) {
         st.nwaited[0] = st.ncommit[0];
         st.nwaited[1] = st.ncommit[1];
@@ -1127,7 +1150,7 @@ __device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int 
 }
 
 // tensor-memory allocation and mbarriers of a CTA (all threads)
-__device__ void mx_setup(MxShared& s, MxState& st) {
+__device__ void mx_setup(MxShared& s, MxState& st, unsigned spin_limit) {
   const int tid = threadIdx.x;
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&s.mbar[0])));
@@ -1147,12 +1170,14 @@ __device__ void mx_setup(MxShared& s, MxState& st) {
   st.ncommit[0] = st.ncommit[1] = 0;
   st.nwaited[0] = st.nwaited[1] = 0;
   st.abort = 0;
+  st.spin = spin_limit;
 }
 
-// every committed MMA must finish before tensor memory is released
+// every committed MMA must finish before tensor memory is released: these
+// waits keep the built-in bound whatever a test set for the pipeline's waits
 __device__ void mx_teardown(MxShared& s, MxState& st) {
   for (int b = 0; b < 2; ++b)
-    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1);
+    if (st.ncommit[b] > st.nwaited[b]) mbar_wait(&s.mbar[b], (st.ncommit[b] - 1) & 1, 0u);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -1258,21 +1283,36 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
 }
 
 __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const __grid_constant__ DecimArgs a,
-                                                            int ns_iter, int ns_final) {
+                                                            int ns_iter, int ns_final,
+                                                            unsigned spin_limit) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
   const MxPlan pl = mx_plan(N, a.w0);
   MxShared s = mx_layout(smraw, pl.wb);
   MxState st;
-  mx_setup(s, st);
+  mx_setup(s, st, spin_limit);
   double2* W = a.ws + (size_t)blockIdx.x * 11 * NN;
   for (;;) {
     if (tid == 0) s.misc[0] = atomicAdd(a.counter, 1);
     __syncthreads();
     const int inst = s.misc[0];
     __syncthreads();
-    if (inst >= a.n_inst || st.abort) break;
+    if (inst >= a.n_inst) break;
     const int ik = inst / a.nomega, iw = inst % a.nomega;
+    if (st.abort) {        // a wait gave up earlier: the rest of this CTA's points are not computed
+      if (tid == 0) {
+        const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
+        const double nan = __longlong_as_double(0x7FF8000000000000LL);
+        a.dos_l[oidx] = nan;
+        a.dos_r[oidx] = nan;
+        a.dos_bulk[oidx] = nan;
+        if (a.spin[0])
+          for (int c = 0; c < 6; ++c) a.spin[c][oidx] = nan;
+        if (a.iters) a.iters[oidx] = 0;
+        if (a.status) a.status[oidx] = (uint8_t)PT_TIMEOUT;
+      }
+      continue;
+    }
     const double2* H00 = a.h + (size_t)ik * 2 * NN;
     const double2* H01 = H00 + NN;
     const double2 w = make_double2(a.omega[iw], a.eta);      // src/surfgreen.f90:82
@@ -1320,12 +1360,13 @@ struct MxOpts {
 // Uneven batch in one persistent launch (mixed form): as k_batch_fp64, with the
 // shared-memory layout sized for the widest B plane of the batch (a.wb).
 __global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__ BatchArgs a,
-                                                         int ns_iter, int ns_final) {
+                                                         int ns_iter, int ns_final,
+                                                         unsigned spin_limit) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int tid = threadIdx.x;
   MxShared s = mx_layout(smraw, a.wb);
   MxState st;
-  mx_setup(s, st);
+  mx_setup(s, st, spin_limit);
   double2* W = a.ws + (size_t)blockIdx.x * a.ws_stride;
   const int npts = a.run ? a.run->npts : a.npts;
   const double tol = a.run ? a.run->tol : a.tol;
@@ -1340,7 +1381,14 @@ __global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__
     const int p = s.misc[0];
     __syncthreads();
     if (p < 0 || st.abort) {
-      if (p >= 0 && tid == 0 && a.status) a.status[p] = PT_TIMEOUT;
+      if (p >= 0 && tid == 0) {       // a wait gave up earlier: not computed
+        const double nan = __longlong_as_double(0x7FF8000000000000LL);
+        a.dos_l[p] = nan;
+        a.dos_r[p] = nan;
+        a.dos_bulk[p] = nan;
+        if (a.iters) a.iters[p] = 0;
+        if (a.status) a.status[p] = PT_TIMEOUT;
+      }
       if (p < 0) break;
       continue;
     }
@@ -1382,7 +1430,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
   MxShared s = mx_layout(smraw, pl.wb);
   const int tid = threadIdx.x;
   MxState st;
-  mx_setup(s, st);
+  mx_setup(s, st, 0u);
   int sing = 0;
   if (op == 0) {
     oz_gemm<OZ_STORE>(X, Y, pl, C, nullptr, nullptr, s, st);
@@ -1439,7 +1487,8 @@ cudaError_t decim_mixed_config(int N, DecimConfig* cfg) {
 
 cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                   cudaStream_t s) {
-  k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 6, 8);
+  k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(
+      a, 6, 8, (unsigned)test_option(WTG_TEST_MIXED_SPIN_LIMIT));
   return cudaGetLastError();
 }
 
@@ -1486,7 +1535,8 @@ cudaError_t batch_mixed_prepare() {
 
 cudaError_t launch_batch_mixed(const BatchArgs& a, const DecimConfig& cfg, int grid,
                                cudaStream_t s) {
-  k_batch_mixed<<<grid, cfg.threads, cfg.smem, s>>>(a, 6, 8);
+  k_batch_mixed<<<grid, cfg.threads, cfg.smem, s>>>(
+      a, 6, 8, (unsigned)test_option(WTG_TEST_MIXED_SPIN_LIMIT));
   return cudaGetLastError();
 }
 

@@ -99,14 +99,18 @@ extern "C" int wtg_surfgreen_batch_noalloc(int ndim, int nw, int nk, const doubl
   wtg::DecimConfig cfg;
   e = wtg::decim_fp64_config(ndim, 0, &cfg);
   if (e != cudaSuccess) return nerr(WTG_ECUDA, std::string("config: ") + cudaGetErrorString(e));
+  if (cfg.ctas_per_sm < 1) return nerr(WTG_EUNSUPPORTED, "decimation kernel does not fit an SM");
   int nsm = 0;
   e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return nerr(WTG_ECUDA, cudaGetErrorString(e));
   const long long n_inst = (long long)nk * nomega;
-  if (n_inst > 0x7fffffffLL) return nerr(WTG_EINVAL, "nk * nomega exceeds 2^31 - 1");
   const size_t fit = (WTG_NOALLOC_SCRATCH_BYTES - counter_bytes) / per_cta;
   long long grid = (long long)cfg.ctas_per_sm * nsm;
   if ((long long)fit < grid) grid = (long long)fit;
+  // every CTA takes one more ticket from the counter after the last instance, so the
+  // counter runs to n_inst + grid: that must stay a valid int
+  if (n_inst > 0x7fffffffLL - grid)
+    return nerr(WTG_EINVAL, "nk * nomega exceeds 2^31 - 1 - " + std::to_string(grid));
   if (n_inst < grid) grid = n_inst;
 
   cudaStream_t s = (cudaStream_t)stream;
