@@ -61,8 +61,10 @@ extern "C" {
                                    119 the inverse runs in global memory) */
 #define WTG_PREC_MIXED 1        /* products as exact BF16 digit splits on the tcgen05 tensor
                                    cores (49-bit operands, FP32 accumulation exact per slice
-                                   order, int64 recombination), inverses FP32 Gauss-Jordan +
-                                   Newton-Schulz refinement on those products; Ndim <= 320 */
+                                   order, int64 recombination); in-loop inverses FP32
+                                   Gauss-Jordan + Newton-Schulz refinement on those products;
+                                   the final GLL / GRR / GB inverses and the convergence norm
+                                   in FP64; Ndim <= 320 */
 
 typedef struct wtg_model* wtg_model_t;
 

@@ -23,12 +23,14 @@
 // Xi [-Yi; Yr], accumulate [Cr | Ci] = [Xr Yr - Xi Yi | Xr Yi + Xi Yr]; both
 // components share one generation of the A planes and every MMA is twice as
 // wide (MxPlan).
-// Inverses (zgesv with identity, src/inverse.f90:43-55) are an FP32
-// Gauss-Jordan (shared memory up to Ndim 112, global memory in panels above)
-// followed by Newton-Schulz refinement X <- X + X (I - M X) whose two products
-// are the split products above, so the inverse reaches the products'
-// accuracy.  Convergence test sum |alpha_ij| (src/surfgreen.f90:120) is
-// evaluated in FP32 from the assembled values.
+// Inverses in the loop (zgesv with identity, src/inverse.f90:43-55) are an
+// FP32 Gauss-Jordan (shared memory up to Ndim 112, global memory in panels
+// above) followed by Newton-Schulz refinement X <- X + X (I - M X): the
+// residual I - M X is a 7-digit split product, the correction X R a 4-digit
+// one (R is small).  The three final inverses (src/surfgreen.f90:127-134) are
+// FP64 Gauss-Jordan (the FP64 form's own code), and the convergence test
+// sum |alpha_ij| (src/surfgreen.f90:120) takes each |alpha_ij| and the sum in
+// FP64.
 //
 // Operands are staged per K chunk of 16 (one MMA k-step) into a double-buffered
 // shared-memory area in the canonical K-major, no-swizzle layout (8 x 16-byte
@@ -72,12 +74,34 @@ constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident c
 // stay below 2^24.
 struct MxPlan {
   int N, NP, nrb, nacc, ncb, w0;
-  int wb;                    // B-plane width of the shared-memory layout (>= w0)
+  int wb;                    // B-plane width of the shared-memory layout
+  int split5;                // order 5 summed in two accumulators, one per K half (K > 256)
+  int lumped;                // the last accumulator sums the orders >= 6 (7-digit products)
 };
 
 // widest pass: both components side by side, 2 x nacc accumulators of w columns
 // in the 512 tensor-memory columns
 __host__ __device__ inline int mx_wmax(int N) { return (512 / (2 * (N > 256 ? 6 : 5))) & ~7; }
+
+// The plan of a 4-digit product (28-bit operands, slice pairs p + q <= 5, every
+// order exact: accumulators for orders 2..5, order 5 split over K halves above
+// K = 256, nothing lumped), used where the product only corrects a value whose
+// size it is small against (the Newton-Schulz update G + G R, |R| << 1).  Its
+// passes are as wide as the tensor memory and the layout's B area (3 NSL wb
+// columns of B planes per buffer) allow.
+__host__ __device__ inline MxPlan mx_plan4(const MxPlan& p7) {
+  MxPlan p = p7;
+  p.nacc = p7.N > 256 ? 5 : 4;
+  p.split5 = p7.N > 256;
+  p.lumped = 0;
+  int wmax = (512 / (2 * p.nacc)) & ~7;
+  const int bcap = ((3 * NSL * p7.wb) / (3 * 4)) & ~7;
+  if (bcap < wmax) wmax = bcap;
+  p.ncb = (p.NP + wmax - 1) / wmax;
+  p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 7) & ~7;
+  while (p.ncb > 1 && (p.ncb - 1) * p.w0 >= p.NP) --p.ncb;
+  return p;
+}
 
 // w0_req: a pass width from the tile table (a multiple of 8 in [8, mx_wmax]); any
 // other value takes the built-in choice (the fewest passes, evenly split)
@@ -87,6 +111,8 @@ __host__ __device__ inline MxPlan mx_plan(int N, int w0_req = 0) {
   p.NP = (N + 15) & ~15;
   p.nrb = (N + 127) / 128;
   p.nacc = N > 256 ? 6 : 5;
+  p.split5 = N > 256;
+  p.lumped = 1;
   const int wmax = mx_wmax(N);
   if (w0_req >= 8 && w0_req <= wmax && (w0_req & 7) == 0) {
     p.w0 = w0_req;
@@ -265,8 +291,29 @@ __host__ __device__ __forceinline__ int bufbytes_of(int WB) {
   return 2 * NSL * APLANE + 3 * NSL * WB * KCH * 2;
 }
 
-// shared-memory layout: two operand buffers (the FP32 Gauss-Jordan matrix
-// aliases them), then the small arrays
+// Bytes of the FP64 Gauss-Jordan working area of the final inverses
+// (fp64_layout with KC = GJ_PANEL): the N x N matrix and its small arrays when
+// the inverse runs in shared memory, the panel arrays when it runs in global
+// memory.
+__host__ __device__ constexpr int fp64_area_bytes(int N, bool in_smem) {
+  return (in_smem ? (N * N > 2 * N * GJ_PANEL ? N * N : 2 * N * GJ_PANEL) : 2 * N * GJ_PANEL) * 16 +
+         N * 32 + 16 * GJ_PANEL + 32 * 8 + N * 8 + 16;
+}
+// the largest over Ndim 1..MX_MAXN (shared-memory inverse up to MX_SMEM_GJ_N)
+constexpr int MX_FP64_AREA =
+    fp64_area_bytes(MX_SMEM_GJ_N, true) > fp64_area_bytes(MX_MAXN, false)
+        ? fp64_area_bytes(MX_SMEM_GJ_N, true) : fp64_area_bytes(MX_MAXN, false);
+
+// bytes before the small arrays: the two operand buffers, which the FP32
+// Gauss-Jordan matrix (or its panel multipliers) and the FP64 final-inverse
+// area alias
+__host__ __device__ __forceinline__ int planes_bytes_of(int WB) {
+  const int two = 2 * bufbytes_of(WB);
+  return ((two > MX_FP64_AREA ? two : MX_FP64_AREA) + 1023) & ~1023;
+}
+
+// shared-memory layout: two operand buffers (the Gauss-Jordan areas alias
+// them), then the small arrays
 __device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int WB) {
   MxShared s;
   const int bb = bufbytes_of(WB);
@@ -274,7 +321,7 @@ __device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int WB) {
   s.buf[1] = smraw + bb;
   s.gj = reinterpret_cast<float2*>(smraw);
   s.mult = reinterpret_cast<float2*>(smraw);
-  unsigned char* tail = smraw + 2 * bb;
+  unsigned char* tail = smraw + planes_bytes_of(WB);
   s.colbuf = reinterpret_cast<float2*>(tail);
   s.rowbuf = s.colbuf + MX_MAXN;
   s.recip = s.rowbuf + MX_MAXN;
@@ -317,12 +364,15 @@ __device__ __forceinline__ void buffer_ready(MxShared& s, MxState& st, int b) {
 }
 
 
-// row exponents of X (over re and im), column exponents of Y: biased-exponent
-// maxima by integer max.  Warp w walks columns w, w+8, ... with its lanes on
-// consecutive rows (coalesced); no integer division.
+// row exponents of X (over re and im) into expA, column exponents of Y into
+// expB: biased-exponent maxima by integer max.  Warp w walks columns w, w+8,
+// ... with its lanes on consecutive rows (coalesced); no integer division.
+// A part whose flag is off keeps what the previous product left (the same
+// operand on the same side).
 __device__ void oz_exponents(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                             MxShared& s) {
+                             MxShared& s, bool rows, bool cols) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  if (rows) {
   for (int r = threadIdx.x; r < MX_MAXN; r += blockDim.x) s.expA[r] = 0;
   __syncthreads();
   int rmax[MX_ROWS];
@@ -346,6 +396,8 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
 #pragma unroll
   for (int m = 0; m < MX_ROWS; ++m)
     if (lane + 32 * m < N) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
+  }
+  if (cols)
   for (int j = warp; j < N; j += 2 * nwarp) {
     const int j1 = j + nwarp;
     const double2* yc0 = Y + (size_t)j * N;
@@ -388,9 +440,9 @@ __host__ __device__ constexpr float pow2f(int e) {
   return e >= 0 ? (float)(1ull << (e < 63 ? e : 62)) : 1.0f / (float)(1ull << (-e));
 }
 
-// the seven digit planes (real and imaginary) of one element pair, stored at
-// dst + plane * pstride (words); scale 2^(7 (e0 - p)) for plane p
-template <int E0>
+// the D (7 or 4) leading digit planes (real and imaginary) of one element
+// pair, stored at dst + plane * pstride (words); scale 2^(7 (e0 - p)) for plane p
+template <int E0, int D>
 __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned long long fr0,
                                            unsigned long long fr1, unsigned long long fi0,
                                            unsigned long long fi1, uint32_t sr, uint32_t si) {
@@ -406,13 +458,17 @@ __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned 
     dst[(2 * (P - 1) + 1) * pstride] =                                                       \
         dig2f(digit7<P>(hi0, li0), digit7<P>(hi1, li1), sc, off, si);                        \
   }
-  WTG_PUT(1) WTG_PUT(2) WTG_PUT(3) WTG_PUT(4) WTG_PUT(5) WTG_PUT(6) WTG_PUT(7)
+  WTG_PUT(1) WTG_PUT(2) WTG_PUT(3) WTG_PUT(4)
+  if constexpr (D > 4) {
+    WTG_PUT(5) WTG_PUT(6) WTG_PUT(7)
+  }
 #undef WTG_PUT
 }
 
 // the B digit planes of one element pair: per digit q the planes -Yi, Yr, Yi
 // (3(q-1), +1, +2), so that [Yr; Yi] and [-Yi; Yr] are each one operand of 2w
-// rows; -Yi is Yi with both BF16 sign bits flipped
+// rows; -Yi is Yi with both BF16 sign bits flipped.  D leading digits (7 or 4).
+template <int D>
 __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigned long long fr0,
                                              unsigned long long fr1, unsigned long long fi0,
                                              unsigned long long fi1, uint32_t sr, uint32_t si) {
@@ -429,7 +485,10 @@ __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigne
     dst[(3 * (P - 1) + 1) * pstride] = br;                                                   \
     dst[(3 * (P - 1) + 2) * pstride] = bi;                                                   \
   }
-  WTG_PUTB(1) WTG_PUTB(2) WTG_PUTB(3) WTG_PUTB(4) WTG_PUTB(5) WTG_PUTB(6) WTG_PUTB(7)
+  WTG_PUTB(1) WTG_PUTB(2) WTG_PUTB(3) WTG_PUTB(4)
+  if constexpr (D > 4) {
+    WTG_PUTB(5) WTG_PUTB(6) WTG_PUTB(7)
+  }
 #undef WTG_PUTB
 }
 
@@ -438,7 +497,8 @@ __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigne
 // Work item `it` covers rows (or columns) 8 (it >> 6) + (lane >> 2) and K pair
 // 8 ((it >> 5) & 1) + 2 (lane & 3); in the canonical layout its word sits at
 // byte 4 it of a plane, so each warp store fills one 128-byte core matrix
-// (no bank conflicts).  Generated by threads gtid = 0 .. gthreads-1.
+// (no bank conflicts).  Generated by threads gtid = 0 .. gthreads-1.  D digits.
+template <int D>
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
                             int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b,
                             int gtid, int gthreads) {
@@ -453,7 +513,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     uint32_t* dst = reinterpret_cast<uint32_t*>(A) + it;
     if (i >= N) {                                  // padding rows of the M = 128 tile
 #pragma unroll
-      for (int pl = 0; pl < 2 * NSL; ++pl) dst[pl * (APLANE / 4)] = 0u;
+      for (int pl = 0; pl < 2 * D; ++pl) dst[pl * (APLANE / 4)] = 0u;
       continue;
     }
     const int E = expA[i];
@@ -463,8 +523,8 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(x0.x, E, n0r), f0i = fixed49(x0.y, E, n0i);
     const unsigned long long f1r = fixed49(x1.x, E, n1r), f1i = fixed49(x1.y, E, n1i);
-    put_digits<3>(dst, APLANE / 4, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
-                  (n0i << 15) | (n1i << 31));
+    put_digits<3, D>(dst, APLANE / 4, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
+                     (n0i << 15) | (n1i << 31));
   }
   for (int it = gtid; it < width * (KCH / 2); it += gthreads) {
     const int cm = it >> 5, ln = it & 31;
@@ -472,7 +532,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     uint32_t* dst = reinterpret_cast<uint32_t*>(B) + it;
     if (j >= N) {                                  // padding columns
 #pragma unroll
-      for (int pl = 0; pl < 3 * NSL; ++pl) dst[pl * bstride] = 0u;
+      for (int pl = 0; pl < 3 * D; ++pl) dst[pl * bstride] = 0u;
       continue;
     }
     const int F = expB[j];
@@ -482,8 +542,8 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(y0.x, F, n0r), f0i = fixed49(y0.y, F, n0i);
     const unsigned long long f1r = fixed49(y1.x, F, n1r), f1i = fixed49(y1.y, F, n1i);
-    put_digits_b(dst, bstride, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
-                 (n0i << 15) | (n1i << 31));
+    put_digits_b<D>(dst, bstride, f0r, f1r, f0i, f1i, (n0r << 15) | (n1r << 31),
+                    (n0i << 15) | (n1i << 31));
   }
 }
 
@@ -495,6 +555,8 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 // of the second K half to accumulator 4) and to the last accumulator for
 // t >= 6; accumulator a sits at tensor-memory column 2 w a.  amask holds the
 // accumulators already written in this pass: the first MMA into one overwrites.
+// D digits: slice pairs p + q <= D + 1.
+template <int D>
 __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int nacc, int khalf,
                          uint32_t& amask) {
   const uint32_t A = saddr(s.buf[b]);
@@ -503,11 +565,11 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int
   const uint64_t adesc0 = sdesc(A), bdesc0 = sdesc(B);
   const uint32_t id2 = idesc(2 * width, 0);
 #pragma unroll 1
-  for (int p = 1; p <= NSL; ++p) {
+  for (int p = 1; p <= D; ++p) {
     const uint64_t aR = adesc0 + (uint64_t)(2 * (p - 1)) * (APLANE >> 4);
     const uint64_t aI = aR + (APLANE >> 4);
 #pragma unroll 1
-    for (int q = 1; q + p <= NSL + 1; ++q) {
+    for (int q = 1; q + p <= D + 1; ++q) {
       const int t = p + q;
       const int a = t <= 4 ? t - 2 : (t == 5 ? 3 + khalf : nacc - 1);
       const uint32_t d = tmem + (uint32_t)(a * 2 * width);
@@ -522,21 +584,32 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int
   }
 }
 
+// |re + i im| in FP64 (Fortran's abs of a complex(dp)); hypot's scaling only
+// outside the range where the squares neither overflow nor underflow
+__device__ __forceinline__ double cabs64(double re, double im) {
+  const double a = fabs(re), b = fabs(im), h = fmax(a, b);
+  if (h < 0x1p500 && h > 0x1p-500) return sqrt(fma(a, a, b * b));
+  return h == 0.0 ? 0.0 : hypot(a, b);
+}
+
 // C = X * Y through the epilogue; returns this thread's partial of sum |C|:
-// OZ_STORE_NORM (the decimation's convergence norm) sums each |C_ij| (to FP32
-// precision) in FP64; OZ_IMINUS (the refinement residual) sums in FP32.
+// OZ_STORE_NORM (the decimation's convergence norm) sums each |C_ij|, both in
+// FP64; OZ_IMINUS (the refinement residual) sums |re| + |im| in FP32.
 // out0/out1/src: FP64 N x N column-major.
-template <int EPI>
+// REUSE bit 0: X is the previous product's X (its row exponents are in expA);
+// bit 1: Y is the previous product's Y (column exponents in expB).
+constexpr int REUSE_X = 1, REUSE_Y = 2;
+template <int EPI, int D = NSL>
 __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y,
                           const MxPlan& pl, double2* out0, double2* out1, const double2* src,
-                          MxShared& s, MxState& st) {
+                          MxShared& s, MxState& st, int reuse = 0) {
   const int N = pl.N, tid = threadIdx.x;
   const int nch = (N + KCH - 1) / KCH;
   const int nacc = pl.nacc, WB = pl.wb;
   const int npass = pl.ncb;
   float nrm = 0.f;
   double nrm_d = 0.0;
-  oz_exponents(X, Y, N, s);
+  oz_exponents(X, Y, N, s, !(reuse & REUSE_X), !(reuse & REUSE_Y));
   __syncthreads();
   for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
     const int rb0 = rb * 128;
@@ -550,7 +623,7 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
         if (tid >= 32) {     // warps 1.. generate while warp 0 issues the previous chunk
           buffer_ready(s, st, b);
           if (!st.abort)
-            oz_generate(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32);
+            oz_generate<D>(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
@@ -558,8 +631,8 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
         tc_fence_after();
         if (st.abort) break;
         if (tid == 0) {
-          const int khalf = (nacc == 6 && 2 * c >= nch) ? 1 : 0;
-          oz_issue(s, st.tmem, b, width, nacc, khalf, amask);
+          const int khalf = (pl.split5 && 2 * c >= nch) ? 1 : 0;
+          oz_issue<D>(s, st.tmem, b, width, nacc, khalf, amask);
           mma_commit(&s.mbar[b]);
         }
         st.ncommit[b] += 1;
@@ -618,7 +691,7 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
 #pragma unroll
                 for (int a = 0; a < 6; ++a) {
                   if (a >= nacc) continue;
-                  if (a == nacc - 1) {
+                  if (pl.lumped && a == nacc - 1) {
                     S += f2ll_bits(v[a][jj]);               // lumped orders >= 6
                   } else {
                     // exact order t: the value is m 2^(56-7t) with |m| < 2^24
@@ -637,14 +710,7 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
                   *(reinterpret_cast<double*>(out1 + idx) + comp) = old1[jj] + val;
                 } else if (EPI == OZ_STORE_NORM) {
                   *o0 = val;
-                  if (comp == 1) {
-                    const float re = fabsf(d2f_bits(old0[jj])), im = fabsf(d2f_bits(val));
-                    const float hi = fmaxf(re, im), lo = fminf(re, im);
-                    if (hi > 0.f) {
-                      const float r = lo / hi;
-                      nrm_d += (double)(hi * sqrtf(fmaf(r, r, 1.f)));
-                    }
-                  }
+                  if (comp == 1) nrm_d += cabs64(old0[jj], val);   // |alpha_ij| in FP64
                 } else if (EPI == OZ_IMINUS) {
                   double w = -val;
                   if (comp == 0 && row == j) w += 1.0;
@@ -1139,7 +1205,8 @@ __device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int 
     const float part = (float)oz_gemm<OZ_IMINUS>(Mi, *Gp, pl, R, nullptr, nullptr, s, st);  // R = I - M G
     const float res = block_sum_f(part, s);
     if (!(res < 0.25f * prev)) break;                 // no longer converging (or NaN)
-    oz_gemm<OZ_ADDTO>(*Gp, R, pl, *Gnp, nullptr, *Gp, s, st);                         // Gn = G + G R
+    // Gn = G + G R: R is small, so 4 digits (28 bits) keep G R far below G's own error
+    oz_gemm<OZ_ADDTO, 4>(*Gp, R, mx_plan4(pl), *Gnp, nullptr, *Gp, s, st);
     double2* tmp = *Gp;
     *Gp = *Gnp;
     *Gnp = tmp;
@@ -1190,11 +1257,15 @@ __device__ void mx_teardown(MxShared& s, MxState& st) {
 // N x N matrices); the spectral sums go to emit(dl, dr, db, spin[6],
 // iterations, status) in thread 0, the final inverses to gll / grr / gb when
 // those are not null.  o has DecimArgs' member names (lists, tolerance, ...).
+// The loop's products and inverses are the split-BF16 forms; the three final
+// inverses (src/surfgreen.f90:127-134) are FP64 Gauss-Jordan, the FP64 form's
+// own (gj_invert in shared memory up to MX_SMEM_GJ_N, gj_invert_global in
+// workspace matrix 8 above), in an area that aliases the idle operand buffers.
 template <class O, class Emit>
-__device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O& o, int ns_iter, int ns_final,
-                            double2* gll, double2* grr, double2* gb, double2* W, MxShared& s,
-                            MxState& st, Emit emit) {
-  const int N = pl.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
+__device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O& o, int ns_iter,
+                                            double2* gll, double2* grr, double2* gb, double2* W,
+                                            MxShared& s, MxState& st, Emit emit) {
+  const int N = pl.N, NN = N * N, tid = threadIdx.x;
   double2* E = W;
   double2* ES = W + (size_t)NN;
   double2* ET = W + (size_t)2 * NN;
@@ -1210,16 +1281,19 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
   bool conv = false;
   for (int itc = 1; itc <= o.itermax && !st.abort; ++itc) {   // src/surfgreen.f90:86-122
     it = itc;
-    // in the loop the refinement may stop at a residual 1000x looser than for the
-    // final inverses: the iteration's products carry it, and the dense Fermi-arc
-    // check stays below 2e-6 against the FP64 oracle
+    // the refinement stops at a residual sum of 1e-4 Ndim (then ~1e-8 after its
+    // update): the dense Fermi-arc check stays below 2e-6 against the FP64 oracle
     if (mixed_inverse(E, w, pl, ns_iter, &G, &Gn, Mi, R, s, st, 1e-4f)) stat |= PT_SINGULAR;
-    oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);
-    oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st);
-    oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);
-    oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st);
-    const double part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st);
-    oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st);
+    // the reference's six products (:92-116), ordered so that each shares an
+    // operand with the one before it and reuses its exponents; eps still
+    // receives M1 beta before M2 alpha
+    oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);                       // :92
+    oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st, REUSE_Y);              // :95
+    oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);                             // :98-102
+    const double part =
+        oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st, REUSE_X);    // :113
+    oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st, REUSE_Y);                    // :107-110
+    oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st, REUSE_X);              // :116
     double2* t0 = Al;
     Al = Gn;
     Gn = t0;
@@ -1233,46 +1307,57 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     }
   }
   if (!conv) stat |= PT_NOT_CONVERGED;
+
+  extern __shared__ __align__(1024) unsigned char smem_dyn[];
+  const bool gsm = N <= MX_SMEM_GJ_N;
+  const Shared fs = fp64_layout(smem_dyn, N, GJ_PANEL, gsm);
+  // (w - X)^-1 in FP64, optionally stored un-permuted to dst; ginv reads the result
+  auto invert = [&](const double2* X, double2* dst) -> int {
+    __syncthreads();                  // the area aliases buffers the loop just used
+    int sing;
+    if (gsm) {
+      sing = gj_invert(X, w, N, fs);
+      if (dst) gj_store(N, fs, dst);
+    } else {
+      sing = gj_invert_global(X, w, N, Mi, fs);
+      if (dst) gj_store_global(N, Mi, fs, dst);
+    }
+    return sing;
+  };
+  auto ginv = [&](int i, int j) {
+    return gsm ? fs.big[i + fs.cols[j] * N] : Mi[i + (size_t)fs.cols[j] * N];
+  };
   double dl = 0.0, dr = 0.0, db = 0.0;
-  if (mixed_inverse(ES, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;  // :127-128
-  if (gll)
-    for (int e = tid; e < NN; e += T) gll[e] = G[e];
   double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (invert(ES, gll)) stat |= PT_SINGULAR;                   // :127-128
   if (tid == 0) {
     for (int q = 0; q < o.ntop; ++q) {
       const int io = o.top[q] - 1;
-      const double v = G[io + (size_t)io * N].y;
+      const double v = ginv(io, io).y;
       dl = o.divide_by_pi ? dl - v / PI_REF : dl - v;
     }
-    if (o.spin[0])
-      spin_sums([&](int i, int j) { return G[i + (size_t)j * N]; }, o.nw, o.ntop, o.top, 0,
-                o.divide_by_pi, spin[0], spin[1], spin[2]);
+    if (o.spin[0]) spin_sums(ginv, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[0], spin[1], spin[2]);
   }
   __syncthreads();
-  if (mixed_inverse(ET, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;  // :130-131
-  if (grr)
-    for (int e = tid; e < NN; e += T) grr[e] = G[e];
+  if (invert(ET, grr)) stat |= PT_SINGULAR;                   // :130-131
   if (tid == 0) {
     for (int q = 0; q < o.nbot; ++q) {
       const int io = N - o.nw + o.bot[q] - 1;
-      const double v = G[io + (size_t)io * N].y;
+      const double v = ginv(io, io).y;
       dr = o.divide_by_pi ? dr - v / PI_REF : dr - v;
     }
     if (o.spin[0]) {
-      auto gr = [&](int i, int j) { return G[i + (size_t)j * N]; };
       if (o.spin_right_bottom)
-        spin_sums(gr, o.nw, o.nbot, o.bot, N - o.nw, o.divide_by_pi, spin[3], spin[4], spin[5]);
+        spin_sums(ginv, o.nw, o.nbot, o.bot, N - o.nw, o.divide_by_pi, spin[3], spin[4], spin[5]);
       else
-        spin_sums(gr, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[3], spin[4], spin[5]);
+        spin_sums(ginv, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[3], spin[4], spin[5]);
     }
   }
   __syncthreads();
-  if (mixed_inverse(E, w, pl, ns_final, &G, &Gn, Mi, R, s, st)) stat |= PT_SINGULAR;   // :133-134
-  if (gb)
-    for (int e = tid; e < NN; e += T) gb[e] = G[e];
+  if (invert(E, gb)) stat |= PT_SINGULAR;                     // :133-134
   if (tid == 0) {
     for (int i = 0; i < N; ++i) {
-      const double v = G[i + (size_t)i * N].y;
+      const double v = ginv(i, i).y;
       db = o.divide_by_pi ? db - v / PI_REF : db - v;
     }
     if (st.abort) stat |= PT_TIMEOUT;
@@ -1283,8 +1368,7 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
 }
 
 __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const __grid_constant__ DecimArgs a,
-                                                            int ns_iter, int ns_final,
-                                                            unsigned spin_limit) {
+                                                            int ns_iter, unsigned spin_limit) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int N = a.N, NN = N * N, T = blockDim.x, tid = threadIdx.x;
   const MxPlan pl = mx_plan(N, a.w0);
@@ -1328,7 +1412,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_decimate_mixed(const __grid_constan
     }
     __syncthreads();
     const size_t oidx = (size_t)(a.k_offset + ik) + (size_t)iw * a.nk_total;
-    mixed_solve(pl, w, a, ns_iter, ns_final, a.gll ? a.gll + (size_t)inst * NN : nullptr,
+    mixed_solve(pl, w, a, ns_iter, a.gll ? a.gll + (size_t)inst * NN : nullptr,
                 a.grr ? a.grr + (size_t)inst * NN : nullptr,
                 a.gb ? a.gb + (size_t)inst * NN : nullptr, W, s, st,
                 [&](double dl, double dr, double db, const double* spin, int it, int stat) {
@@ -1360,8 +1444,7 @@ struct MxOpts {
 // Uneven batch in one persistent launch (mixed form): as k_batch_fp64, with the
 // shared-memory layout sized for the widest B plane of the batch (a.wb).
 __global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__ BatchArgs a,
-                                                         int ns_iter, int ns_final,
-                                                         unsigned spin_limit) {
+                                                         int ns_iter, unsigned spin_limit) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   const int tid = threadIdx.x;
   MxShared s = mx_layout(smraw, a.wb);
@@ -1407,7 +1490,7 @@ __global__ void __launch_bounds__(MX_T, 1) k_batch_mixed(const __grid_constant__
     o.bot = m.bot;
     for (int c = 0; c < 6; ++c) o.spin[c] = nullptr;
     o.spin_right_bottom = 0;
-    mixed_solve(pl, make_double2(a.omega[p], a.eta[p]), o, ns_iter, ns_final, nullptr, nullptr,
+    mixed_solve(pl, make_double2(a.omega[p], a.eta[p]), o, ns_iter, nullptr, nullptr,
                 nullptr, W, s, st,
                 [&](double dl, double dr, double db, const double*, int it, int stat) {
                   a.dos_l[p] = dl;
@@ -1451,12 +1534,12 @@ __global__ void __launch_bounds__(MX_T, 1) k_mixed_unit(int op, int N, const dou
 
 size_t mixed_smem(int N, int wb = 0) {     // wb = 0: the built-in plan's width
   const MxPlan pl = mx_plan(N);
-  const size_t bufbytes = (size_t)bufbytes_of(wb > 0 ? wb : pl.w0);
-  // the FP32 Gauss-Jordan matrix ((N+1)*N float2, Ndim <= MX_SMEM_GJ_N) or the
-  // multiplier columns (MX_MAXN * MX_PANEL float2, reserved twice) alias the buffers
-  size_t planes = 2 * bufbytes;
-  const size_t gj = N <= MX_SMEM_GJ_N ? (size_t)(N + 1) * N * 8 : (size_t)2 * MX_MAXN * MX_PANEL * 8;
-  if (gj > planes) planes = gj;
+  // the FP32 Gauss-Jordan matrix ((N+1)*N float2, Ndim <= MX_SMEM_GJ_N), its
+  // multiplier columns (MX_MAXN * MX_PANEL float2, reserved twice) and the FP64
+  // area of the final inverses all fit the planes region
+  static_assert((MX_SMEM_GJ_N + 1) * MX_SMEM_GJ_N * 8 <= MX_FP64_AREA, "FP32 GJ area");
+  static_assert(2 * MX_MAXN * MX_PANEL * 8 <= MX_FP64_AREA, "FP32 GJ panel area");
+  const size_t planes = (size_t)planes_bytes_of(wb > 0 ? wb : pl.w0);
   return planes + (size_t)MX_MAXN * 8 * 2 + MX_PANEL * 8 + (size_t)MX_MAXN * 4 * 4 + 32 * 4 +
          16 + 8 + 16;
 }
@@ -1488,7 +1571,7 @@ cudaError_t decim_mixed_config(int N, DecimConfig* cfg) {
 cudaError_t launch_decimate_mixed(const DecimArgs& a, const DecimConfig& cfg, int grid,
                                   cudaStream_t s) {
   k_decimate_mixed<<<grid, cfg.threads, cfg.smem, s>>>(
-      a, 6, 8, (unsigned)test_option(WTG_TEST_MIXED_SPIN_LIMIT));
+      a, 6, (unsigned)test_option(WTG_TEST_MIXED_SPIN_LIMIT));
   return cudaGetLastError();
 }
 
@@ -1536,7 +1619,7 @@ cudaError_t batch_mixed_prepare() {
 cudaError_t launch_batch_mixed(const BatchArgs& a, const DecimConfig& cfg, int grid,
                                cudaStream_t s) {
   k_batch_mixed<<<grid, cfg.threads, cfg.smem, s>>>(
-      a, 6, 8, (unsigned)test_option(WTG_TEST_MIXED_SPIN_LIMIT));
+      a, 6, (unsigned)test_option(WTG_TEST_MIXED_SPIN_LIMIT));
   return cudaGetLastError();
 }
 
