@@ -223,8 +223,13 @@ int wtg_model_profile_read(wtg_model_t model, double* fourier_ms, double* decim_
                            long long* launches, int* decim_launches);
 
 /* FP64 (DFMA) throughput of the current device in TFLOP/s: the roofline
-   denominator of the FP64 path, measured with a short throughput kernel. */
+   denominator of the FP64 path, measured with a short throughput kernel.
+   No counterpart in the reference. */
 int wtg_probe_fp64_peak(double* tflops);
+/* FP64 tensor-core (mma.sync m8n8k4 .f64, DMMA) throughput of the current
+   device in TFLOP/s, measured the same way: the rate a zgemm on the FP64
+   tensor path (src/mat_mul.f90:23 through a tensor-core BLAS) could reach. */
+int wtg_probe_dmma_peak(double* tflops);
 
 /*
  * Allocation-free batched decimation.  No counterpart in the reference: it

@@ -215,3 +215,11 @@ def test_spin_resolved_spectra(lib, nw, np_, arc):
     for name in ("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r"):
         scale = np.abs(ref["dos_l"]).max()
         assert np.max(np.abs(got[name] - ref[name])) <= 1e-9 * scale, name
+
+
+def test_fp64_throughput_probes(built_lib):
+    """The live roofline denominators: DFMA and DMMA rates are positive and of the
+    order of a GB300's FP64 rate (about 1.2 TFLOP/s)."""
+    dfma, dmma = api.fp64_peak_tflops(), api.dmma_peak_tflops()
+    print("FP64 DFMA %.3f TFLOP/s, DMMA %.3f TFLOP/s" % (dfma, dmma))
+    assert 0.2 < dfma < 20 and 0.2 < dmma < 20

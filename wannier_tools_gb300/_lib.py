@@ -62,6 +62,7 @@ SIGNATURES = {
     "wtg_model_profile": (C.c_int, [_vp, C.c_int]),
     "wtg_model_profile_read": (C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_longlong), _ip]),
     "wtg_probe_fp64_peak": (C.c_int, [_dp]),
+    "wtg_probe_dmma_peak": (C.c_int, [_dp]),
     "wtg_surfgreen_batch_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_double,
                                                C.c_double, C.c_int, C.c_int, _ip, C.c_int, _ip, C.c_int,
                                                _vp, _vp, _vp, _vp, _vp, _vp]),

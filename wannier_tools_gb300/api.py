@@ -528,3 +528,10 @@ def fp64_peak_tflops() -> float:
     check(_lib.load().wtg_probe_fp64_peak(C.byref(v)))
     return float(v.value)
 
+
+def dmma_peak_tflops() -> float:
+    """FP64 tensor-core (DMMA) throughput of the current GPU (wtg_probe_dmma_peak)."""
+    v = C.c_double(0.0)
+    check(_lib.load().wtg_probe_dmma_peak(C.byref(v)))
+    return float(v.value)
+
