@@ -756,7 +756,7 @@ def serve_measure(wl, prec, rates, requests, warm=3):
                        max_slots=wl["slots"]) as srv:
         replay(srv, poisson_requests(np.random.default_rng(1), len(ms), 1e3, warm), EV2HARTREE)
         torch.cuda.synchronize()
-        l0 = sum(e.info()["launches"] for e in srv.engines)
+        l0 = srv.launches()
         with ClockSampler(0) as clk:
             for i, rate in enumerate(rates):
                 reqs = poisson_requests(np.random.default_rng(wl["seed"] + i), len(ms), rate, requests)
@@ -764,8 +764,8 @@ def serve_measure(wl, prec, rates, requests, warm=3):
                 rep.pop("results")
                 rep["rate_per_s"] = rate
                 sweep.append(rep)
-        launches = sum(e.info()["launches"] for e in srv.engines) - l0
-        nslots = len(srv.engines)
+        launches = srv.launches() - l0
+        nslots = srv.engines_built
     for g in gs:
         g.close()
     return {"sweep": sweep, "clocks": clk.summary(), "launches": launches, "slots": nslots}
@@ -780,7 +780,8 @@ def serve_config():
     fp64 = serve_measure(wl, PREC_FP64, (1000.0,), wl["fp64_requests"])
     best = max(mixed["sweep"], key=lambda x: x["solves_per_s"])
     f = fp64["sweep"][0]
-    return {"workload": wl["desc"], "slots": mixed["slots"], "slot_points": wl["slot_points"],
+    return {"workload": wl["desc"], "engines_built": mixed["slots"], "max_engines": wl["slots"],
+            "slot_points": wl["slot_points"],
             "timing": "wall clock from first arrival to last completion of each replay",
             "mixed": {"value": best["solves_per_s"], "requests_per_rate": wl["requests"],
                       "sweep": [{k: x[k] for k in ("rate_per_s", "requests", "points", "wall_s",
@@ -814,7 +815,8 @@ def run_serve(args):
             "ms_per_step": 1e3 * sum(x["wall_s"] for x in r["sweep"]) / len(r["sweep"]),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": wl["desc"], "precision": forms[0], "slots": r["slots"],
+            "config": {"workload": wl["desc"], "precision": forms[0], "engines_built": r["slots"],
+                       "max_engines": wl["slots"],
                        "slot_points": wl["slot_points"], "requests_per_rate": nreq,
                        "step": "one Poisson replay at one rate; value = best served solves/s",
                        "timing": "wall clock from first arrival to last completion"},

@@ -144,3 +144,28 @@ def test_serving_alone_equals_in_mix(models, prec):
     ref = gs[reqs[5][0]].surface_spectrum(reqs[5][1], reqs[5][2], reqs[5][3], tops[reqs[5][0]],
                                           bots[reqs[5][0]], precision=prec)
     assert rel(alone["dos_bulk"], ref["dos_bulk"][0]) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_MIXED])
+def test_serving_model_added_while_running(models, prec):
+    """A model registered while requests are in flight is served by an engine built
+    after it, with the per-model path's result (1e-12; the same per-point arithmetic)."""
+    from wannier_tools_gb300.serving import SurfaceServer
+    ms, gs = models
+    tops, bots = _lists(ms)
+    extra = synthetic.make_model(30, 2, seed=777)                  # Ndim 60
+    with api.Model.from_surface_model(extra) as g_extra:
+        with SurfaceServer(gs[:2], tops[:2], bots[:2], precision=prec, slot_points=128,
+                           max_slots=2) as srv:
+            busy = [srv.submit(i % 2, [[0.1 * i, 0.2]], np.linspace(-0.5, 0.5, 60) * EV, 5e-3 * EV)
+                    for i in range(4)]
+            mid = srv.add_model(g_extra, list(range(1, 31, 2)), list(range(1, 31, 3)))
+            om = np.linspace(-0.3, 0.4, 50) * EV
+            got = srv.submit(mid, [[0.25, -0.1]], om, 4e-3 * EV).result(timeout=600)
+            for f in busy:
+                assert (f.result(timeout=600)["status"] == 0).all()
+            assert srv.engines_built >= 2
+        ref = g_extra.surface_spectrum([[0.25, -0.1]], om, 4e-3 * EV, list(range(1, 31, 2)),
+                                       list(range(1, 31, 3)), precision=prec)
+    for name in ("dos_l", "dos_r", "dos_bulk"):
+        assert rel(got[name], ref[name][0]) <= 1e-12, name
