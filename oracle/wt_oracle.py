@@ -454,6 +454,46 @@ def get_hmnr_cell_identity(irvec, ndegen, hmnr, max_ir=8):
     return np.array(order, np.int32).reshape(-1, 3), np.ones(len(order), np.int32), out
 
 
+def get_hmnr_cell(irvec, ndegen, hmnr, umatrix, orb_atom, pos_old, pos_new, max_ir=8):
+    """get_hmnr_cell (src/readHmnR.f90:578-766) for any SURFACE card, step by step:
+    for every (ir, j, i) (:624-645), Rmn = irvec + tau(atom j) - tau(atom i) in the
+    original cell (:636), latticetransform (src/ham_qlayer2qlayer.f90:817-838:
+    x_c = sum_r Rmn_r Uinv(r, c)), minus tau'(atom j) - tau'(atom i) in the surface
+    cell (:638), ANINT (:641-643), the |R'| <= max_ir cut (:645); R' ordered by
+    nested loops nir3, nir2, nir1 (:663-674); HmnR/ndegen assigned (a later
+    (ir, i, j) replaces an earlier one, :720); ndegen_surfacecell = 1 (:681).
+    orb_atom: 0-based atom of each orbital; positions in direct coordinates."""
+    uinv = np.linalg.inv(np.asarray(umatrix, dtype=float))
+    nw = hmnr.shape[1]
+
+    def anint(x):
+        return int(math.copysign(math.floor(abs(x) + 0.5), x))
+
+    def new_r(ir, i, j):
+        rmn = [float(irvec[ir][c]) + pos_old[orb_atom[j]][c] - pos_old[orb_atom[i]][c] for c in range(3)]
+        x = [sum(rmn[r] * uinv[r][c] for r in range(3)) for c in range(3)]
+        return tuple(anint(x[c] - (pos_new[orb_atom[j]][c] - pos_new[orb_atom[i]][c])) for c in range(3))
+
+    rpts = set()
+    for ir in range(irvec.shape[0]):
+        for j in range(nw):
+            for i in range(nw):
+                v = new_r(ir, i, j)
+                if max(abs(v[0]), abs(v[1]), abs(v[2])) <= max_ir:
+                    rpts.add(v)
+    order = [(n1, n2, n3) for n3 in range(-max_ir, max_ir + 1) for n2 in range(-max_ir, max_ir + 1)
+             for n1 in range(-max_ir, max_ir + 1) if (n1, n2, n3) in rpts]
+    rmap = {v: k for k, v in enumerate(order)}
+    out = np.zeros((len(order), nw, nw), np.complex128)
+    for ir in range(irvec.shape[0]):
+        for j in range(nw):
+            for i in range(nw):
+                v = new_r(ir, i, j)
+                if v in rmap:
+                    out[rmap[v], i, j] = hmnr[ir, i, j] / ndegen[ir]
+    return np.array(order, np.int32).reshape(-1, 3), np.ones(len(order), np.int32), out
+
+
 def chain_surface_gf(z, e0, t):
     """Closed-form retarded surface and bulk Green's functions of the
     semi-infinite 1-D chain (onsite e0, hopping t): g solves

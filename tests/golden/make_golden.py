@@ -8,6 +8,9 @@ reads examples/3DWeyl-model/Weyl3D_hr.dat from it):
 Fixtures:
   weyl3d_hr_model.npz    the reference's 2-band Weyl model (examples/3DWeyl-model/
                          Weyl3D_hr.dat, eV), parsed as readNormalHmnR does.
+  weyl3d_wt.in           the same example's surface-state input file
+                         (examples/3DWeyl-model/wt.in-surfacestates), copied
+                         unchanged: the drop-in test runs it.
   analytic_chain.npz     closed-form surface / bulk Green's functions of the
                          semi-infinite chain (independent of any code here).
   oracle_weyl3d.npz      oracle outputs (H00/H01 at one k; dos_l/dos_r/dos_bulk
@@ -36,7 +39,13 @@ from wannier_tools_gb300 import hrfile, synthetic  # noqa: E402
 HERE = Path(__file__).resolve().parent
 
 
+def copy_inputs(ref_root: str) -> None:
+    src = Path(ref_root) / "examples/3DWeyl-model/wt.in-surfacestates"
+    (HERE / "weyl3d_wt.in").write_text(src.read_text())
+
+
 def main(ref_root: str) -> None:
+    copy_inputs(ref_root)
     hr = hrfile.read_hr(Path(ref_root) / "examples/3DWeyl-model/Weyl3D_hr.dat")
     np.savez(HERE / "weyl3d_hr_model.npz", irvec=hr["irvec"], ndegen=hr["ndegen"], hmnr_ev=hr["hmnr"])
 

@@ -7,11 +7,17 @@
                       (src/readHmnR.f90:100-125).
 * ``to_hartree``      E_fermi removed from the R = 0 diagonal and eV -> Hartree
                       (src/readHmnR.f90:141-159).
-* ``surface_cell``    get_hmnr_cell (src/readHmnR.f90:578-766) for a SURFACE
-                      card that keeps the lattice (identity Umatrix, the (001)
-                      default of src/readinput.f90:1594-1598): R' = R, the
-                      |R'| <= 8 cut-off, R' ordered R1 fastest then R2 then R3,
-                      values divided by ndegen and ndegen set to 1.
+* ``get_hmnr_cell``   the surface-cell remap of src/readHmnR.f90:578-766 for any
+                      SURFACE card: each hopping H_ij(R) moves to
+                      R' = U^-T (R + tau_j - tau_i) - (tau'_j - tau'_i), rounded
+                      half away from zero (ANINT), the orbitals' atoms at tau in
+                      the original cell and tau' in the surface cell; R' with a
+                      component beyond 8 is dropped; R' ordered R1 fastest then
+                      R2 then R3; values divided by ndegen, which becomes 1; a
+                      later (R, i, j) mapped to the same (R', i, j) replaces an
+                      earlier one, as the reference's assignment does.
+* ``surface_cell``    the same for a SURFACE card that keeps the lattice and
+                      every orbital at the origin (R' = R).
 * ``write_hr``        the wannier90_hr.dat text layout (as written for
                       wannier90_hr_newcell.dat, src/readHmnR.f90:738-758).
 """
@@ -68,6 +74,49 @@ def to_hartree(hr: dict, e_fermi_ev: float = 0.0) -> dict:
             h[r][np.diag_indices(h.shape[1])] -= e_fermi_ev
     out["hmnr"] = h * EV2HARTREE
     return out
+
+
+def _anint(x: np.ndarray) -> np.ndarray:
+    """Fortran ANINT: nearest integer, halves away from zero."""
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def get_hmnr_cell(hr: dict, umatrix, orb_atom, pos_old, pos_new, max_ir: int = MAX_IR) -> dict:
+    """HmnR of the cell defined by the SURFACE card (see module docstring).
+
+    hr        irvec (nR, 3), ndegen (nR,), hmnr (nR, nw, nw)
+    umatrix   3 x 3, rows R1', R2', R3' in units of the original lattice vectors
+    orb_atom  (nw,) 0-based atom of each orbital (the same in both cells)
+    pos_old   (natoms, 3) direct coordinates in the original cell
+    pos_new   (natoms, 3) direct coordinates in the surface cell
+    """
+    irv = np.asarray(hr["irvec"], dtype=np.float64)
+    h = np.asarray(hr["hmnr"])
+    nd = np.asarray(hr["ndegen"], dtype=np.float64)
+    nR, nw, _ = h.shape
+    uinv_t = np.linalg.inv(np.asarray(umatrix, dtype=np.float64)).T
+    ta = np.asarray(pos_old, dtype=np.float64)[np.asarray(orb_atom)]       # (nw, 3)
+    tb = np.asarray(pos_new, dtype=np.float64)[np.asarray(orb_atom)]
+    dold = ta[None, :, :] - ta[:, None, :]          # [i, j] = tau_j - tau_i
+    dnew = tb[None, :, :] - tb[:, None, :]
+    rnew = np.empty((nR, nw, nw, 3), dtype=np.int64)
+    for r in range(nR):
+        rmn = irv[r][None, None, :] + dold
+        rnew[r] = _anint(rmn @ uinv_t.T - dnew).astype(np.int64)
+    keep = np.all(np.abs(rnew) <= max_ir, axis=-1)
+    present = np.unique(rnew[keep].reshape(-1, 3), axis=0)
+    order = present[np.lexsort((present[:, 0], present[:, 1], present[:, 2]))]
+    span = 2 * max_ir + 1
+    key = lambda v: ((v[..., 2] + max_ir) * span + (v[..., 1] + max_ir)) * span + (v[..., 0] + max_ir)
+    slot = np.full(span ** 3, -1, dtype=np.int64)
+    slot[key(order)] = np.arange(len(order))
+    out = np.zeros((len(order), nw, nw), dtype=np.complex128)
+    ii, jj = np.meshgrid(np.arange(nw), np.arange(nw), indexing="ij")
+    for r in range(nR):                              # in R order: later entries replace earlier
+        k = keep[r]
+        out[slot[key(rnew[r][k])], ii[k], jj[k]] = h[r][k] / nd[r]
+    return {"nw": nw, "irvec": order.astype(np.int32).reshape(-1, 3),
+            "ndegen": np.ones(len(order), np.int32), "hmnr": out}
 
 
 def surface_cell(hr: dict) -> dict:
