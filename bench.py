@@ -286,7 +286,7 @@ class SpectrumRun:
     device inputs/outputs for the CUDA-event timing, pinned host buffers for the
     host-buffer (e2e) call."""
 
-    def __init__(self, wl, dev, ws=1, rank=0, batch=0, nslabs=8):
+    def __init__(self, wl, dev, ws=1, rank=0, batch=0, nslabs=8, nomega=0):
         import numpy as np
         import torch
 
@@ -296,6 +296,8 @@ class SpectrumRun:
         self.m = w.make_model(wl["nw"], wl["np_"], seed=wl["seed"])
         self.model = w.Model.from_surface_model(self.m)
         self.k_all, self.om = workload_points(wl)
+        if 0 < nomega < len(self.om):        # a smaller step: evenly strided omegas of the list
+            self.om = self.om[np.linspace(0, len(self.om) - 1, nomega).round().astype(int)]
         self.top, self.bot = orbitals(wl)
         self.nomega = len(self.om)
         nsm = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -478,7 +480,7 @@ def run_gpu(args):
     w.build()
     dev = torch.device("cuda", local)
     nsteps = args.warmup + args.steps
-    run = SpectrumRun(wl, dev, ws, rank, args.batch, nslabs=nsteps)
+    run = SpectrumRun(wl, dev, ws, rank, args.batch, nslabs=nsteps, nomega=args.nomega)
     precs = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
     primary = args.precision
     forms = [primary] + ([] if args.only else [p for p in ("fp64", "mixed") if p != primary])
@@ -900,6 +902,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="arc_n112")
     ap.add_argument("--batch", type=int, default=0, help="k points per step (0 = 8 x SMs)")
+    ap.add_argument("--nomega", type=int, default=0,
+                    help="omegas per k point: this many evenly strided ones of the workload's list "
+                         "(0 = all); with --batch, a smaller launch of the same kernel")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="default workload only: leave out the `configs` runs of the other workloads")
