@@ -48,6 +48,16 @@ struct SolveOpts {
   int spin_right_bottom;
 };
 
+// The products of one decimation step.  At the large Ndim of the global-memory
+// inverse the eight workspaces of all resident CTAs no longer fit the L2, so
+// operands come from DRAM and their staging is double-buffered.
+template <int RP, int EPI, bool GI>
+__device__ __forceinline__ double gemm(const double2* X, const double2* Y, int N, int KC,
+                                       const Shared& s, double2* out0, double2* out1) {
+  if (GI) return cta_gemm_db<RP, EPI>(X, Y, N, KC, s.sX, out0, out1);
+  return cta_gemm<RP, EPI>(X, Y, N, KC, s.sX, s.sY, out0, out1);
+}
+
 // Decimation of one instance whose eps, eps_s, eps_t (= H00), alpha (= H01)
 // and beta (= H01^dagger) already sit in workspace matrices 0..4 of W; the
 // spectral sums of the three final inverses are handed to emit(dl, dr, db,
@@ -91,12 +101,12 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
     it = itc;
     if (invert(E, G)) st |= PT_SINGULAR;                      // :88-89
     __syncthreads();
-    cta_gemm<RP, EPI_STORE>(Al, G, N, KC, s.sX, s.sY, M1, nullptr);     // :92
-    cta_gemm<RP, EPI_STORE>(Be, G, N, KC, s.sX, s.sY, M2, nullptr);     // :95
-    cta_gemm<RP, EPI_ADD2>(M1, Be, N, KC, s.sX, s.sY, E, ES);           // :98-102
-    cta_gemm<RP, EPI_ADD2>(M2, Al, N, KC, s.sX, s.sY, E, ET);           // :107-110
-    double part = cta_gemm<RP, EPI_STORE_NORM>(M1, Al, N, KC, s.sX, s.sY, G, nullptr);  // :113
-    cta_gemm<RP, EPI_STORE>(M2, Be, N, KC, s.sX, s.sY, M1, nullptr);    // :116
+    gemm<RP, EPI_STORE, GI>(Al, G, N, KC, s, M1, nullptr);              // :92
+    gemm<RP, EPI_STORE, GI>(Be, G, N, KC, s, M2, nullptr);              // :95
+    gemm<RP, EPI_ADD2, GI>(M1, Be, N, KC, s, E, ES);                    // :98-102
+    gemm<RP, EPI_ADD2, GI>(M2, Al, N, KC, s, E, ET);                    // :107-110
+    double part = gemm<RP, EPI_STORE_NORM, GI>(M1, Al, N, KC, s, G, nullptr);  // :113
+    gemm<RP, EPI_STORE, GI>(M2, Be, N, KC, s, M1, nullptr);             // :116
     // rotate buffers: alpha <- G, beta <- M1
     double2* t0 = Al;
     Al = G;

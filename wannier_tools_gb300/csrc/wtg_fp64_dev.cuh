@@ -78,6 +78,109 @@ __device__ double cta_gemm(const double2* __restrict__ X, const double2* __restr
   return nrm;
 }
 
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(NPEND) : "memory");
+}
+
+// cta_gemm for operands that live in DRAM (the large-Ndim workspaces exceed the
+// L2): the same shared area (2 N KC double2) holds two stages of KS = KC / 2
+// columns, filled with cp.async, so that the next K chunk loads while the
+// current one is computed instead of between two barriers.  Every output sums
+// the same products in the same (ascending k) order as cta_gemm: the results
+// are bit-identical.
+template <int RP, int EPI>
+__device__ double cta_gemm_db(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
+                              int KC, double2* stages, double2* out0, double2* out1) {
+  const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
+  const int KS = KC / 2;
+  const int nch = (N + KS - 1) / KS;
+  const int rounds = (NN + T - 1) / T;
+  double nrm = 0.0;
+  auto stage = [&](int c) {
+    const int k0 = c * KS, kc = min(KS, N - k0);
+    double2* sx = stages + (size_t)(c & 1) * 2 * N * KS;
+    double2* sy = sx + (size_t)N * KS;
+    const double2* Xc = X + (size_t)k0 * N;          // columns k0.. are contiguous
+    for (int e = tid; e < N * kc; e += T) cp_async16(sx + e, Xc + e);
+    for (int e = tid; e < N * kc; e += T) {
+      const int kk = e % kc, j = e / kc;
+      cp_async16(sy + kk + j * KS, Y + (k0 + kk) + (size_t)j * N);
+    }
+    cp_async_commit();
+  };
+  for (int r0 = 0; r0 < rounds; r0 += RP) {
+    const int nr = min(RP, rounds - r0);
+    int oa[RP], ob[RP];
+    double2 acc[RP];
+#pragma unroll
+    for (int r = 0; r < RP; ++r) {
+      const int idx = tid + (r0 + r) * T;
+      int i = 0, j = 0;
+      if (idx < NN) {
+        i = idx % N;
+        j = idx / N;
+      }
+      oa[r] = i;
+      ob[r] = j * KS;
+      acc[r] = make_double2(0.0, 0.0);
+    }
+    stage(0);
+    for (int c = 0; c < nch; ++c) {
+      if (c + 1 < nch) {
+        stage(c + 1);                 // its buffer was last read before the previous barrier
+        cp_async_wait<1>();           // this thread's copies of chunk c have landed
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();                // everyone's copies of chunk c are visible
+      const int kc = min(KS, N - c * KS);
+      const double2* sx = stages + (size_t)(c & 1) * 2 * N * KS;
+      const double2* sy = sx + (size_t)N * KS;
+      for (int kk = 0; kk < kc; ++kk) {
+        const double2* xr = sx + kk * N;
+        const double2* yr = sy + kk;
+#pragma unroll
+        for (int r = 0; r < RP; ++r) {
+          if (r < nr) cfma(acc[r], xr[oa[r]], yr[ob[r]]);
+        }
+      }
+      __syncthreads();                // chunk c's buffer may be refilled
+    }
+#pragma unroll
+    for (int r = 0; r < RP; ++r) {
+      const int idx = tid + (r0 + r) * T;
+      if (r < nr && idx < NN) {
+        if (EPI == EPI_STORE) {
+          out0[idx] = acc[r];
+        } else if (EPI == EPI_ADD2) {
+          double2 v = out0[idx];
+          v.x += acc[r].x;
+          v.y += acc[r].y;
+          out0[idx] = v;
+          double2 w = out1[idx];
+          w.x += acc[r].x;
+          w.y += acc[r].y;
+          out1[idx] = w;
+        } else {
+          out0[idx] = acc[r];
+          nrm += sqrt(acc[r].x * acc[r].x + acc[r].y * acc[r].y);
+        }
+      }
+    }
+  }
+  return nrm;
+}
+
 constexpr int GJ_PANEL = 8;   // pivot steps per pass of the global-memory Gauss-Jordan
 
 struct Shared {
