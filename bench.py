@@ -11,6 +11,9 @@ reports the all-FP64 form as `value` and the mixed (split-BF16 tensor-core)
 form beside it, and carries a `configs` object with the other workloads, each
 run for a bounded number of steps stated inside it:
 
+  plane    the whole 201 x 201 plane of the default workload in one public-API
+           call per form (host buffers), and the two forms' agreement over every
+           one of its 40 401 points
   ss_n264  the k-path x omega spectrum at Ndim 264 (Num_wann 88, Np 3), 301 k x
            501 omega in [-0.5, 0.5] eV, eta 1e-3 eV: both forms, e2e, errors
   uneven4  four models of Ndim 16 / 40 / 112 / 264 interleaved in one persistent
@@ -510,7 +513,8 @@ def run_gpu(args):
     configs = None
     if rank == 0 and ws == 1 and args.workload == "arc_n112" and not args.no_configs:
         configs = {}
-        for name, fn in (("ss_n264", lambda: ss_n264_config(dev, pool, ncores, peaks)),
+        for name, fn in (("plane", lambda: plane_config(run)),
+                         ("ss_n264", lambda: ss_n264_config(dev, pool, ncores, peaks)),
                          ("uneven4", lambda: uneven_config(pool, ncores)),
                          ("serve8", serve_config)):
             t0 = time.perf_counter()
@@ -553,6 +557,39 @@ def run_gpu(args):
         pool.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def plane_config(run):
+    """The whole configuration end to end: every k point of the workload (all 40 401 points of
+    the 201 x 201 arc plane) in one public-API call per form, host k list in and host DOS out,
+    and the two forms' agreement over every point of the plane (a full-size check beside the
+    sampled oracle errors of the line)."""
+    import numpy as np
+    import torch
+
+    from wannier_tools_gb300._lib import PREC_FP64, PREC_MIXED
+    wl, dev = run.wl, run.dev
+    npts = len(run.k_all) * run.nomega
+    out = {"workload": wl["desc"], "points": npts,
+           "timing": "wall clock around one surface_spectrum call over every k point (host k "
+                     "list in, host dos_l / dos_r / dos_bulk / iters / status out)"}
+    res = {}
+    for f, prec in (("mixed", PREC_MIXED), ("fp64", PREC_FP64)):
+        run.flush.zero_()
+        torch.cuda.synchronize(dev)
+        with ClockSampler(dev.index or 0) as clk:
+            t0 = time.perf_counter()
+            g = run.model.surface_spectrum(run.k_all, run.om, run.eta, run.top, run.bot, tol=run.tol,
+                                           divide_by_pi=wl["divide_by_pi"], precision=prec)
+            dt = time.perf_counter() - t0
+        res[f] = g
+        out[f] = {"value": npts / dt, "unit": "solves/s", "wall_s": dt,
+                  "mean_iterations": float(g["iters"].mean()),
+                  "status_flagged_points": int((g["status"] != 0).sum()), "clocks": clk.summary()}
+    out["mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["mixed_max_rel_diff_vs_fp64"] = max_rel(res["mixed"], res["fp64"])
+    out["fp64_sums"] = {name: float(np.sum(res["fp64"][name])) for name in NAMES}
+    return out
 
 
 def ss_n264_config(dev, pool, ncores, peaks):
