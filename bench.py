@@ -422,12 +422,12 @@ class SpectrumRun:
                     "dfma_peak": peaks["dfma"], "dmma_peak": peaks["dmma"], "launch_ms": launch_ms,
                     "work": "(56*it+24)*Ndim^3 flops per solve, it = FP64 iterations"}
         m = self.m
-        npad = (m.ndim + 15) // 16 * 16
+        npad = (m.ndim + 7) // 8 * 8
         nch = (m.ndim + 15) // 16
         nrb = (m.ndim + 127) // 128
         # BF16 MMA flops issued by one 7-digit complex product: row blocks of 128 x 2
         # components x K chunks x 28 slice pairs x 2 real products x 2*128*16 flops per
-        # output column over Ndim16 columns; 7 such products per iteration (six loop products
+        # output column over Ndim columns rounded up to 8; 7 such products per iteration (six loop products
         # and the refinement's residual), the 4-digit correction (10 pairs) as 10/28 of one
         per_prod = nrb * 2 * nch * 56 * 2.0 * 128 * 16 * npad
         issued = float(((7.0 + 10.0 / 28.0) * its * per_prod).sum())
@@ -440,7 +440,7 @@ class SpectrumRun:
                 "issued_bf16_tflops": iss, "issued_frac": (iss / peak) if (iss and peak) else None,
                 "issued_work": "BF16 MMA flops issued: per iteration 7 products of 28 slice pairs and "
                                "one of 10, each ceil(Ndim/128) row blocks x 2 components x "
-                               "ceil(Ndim/16) K chunks x 2*128*16 flops per column x Ndim16 columns",
+                               "ceil(Ndim/16) K chunks x 2*128*16 flops per column x Ndim columns rounded up to 8",
                 "vs_fp64_peak": (ach / max(peaks["dfma"], peaks["dmma"])) if ach else None}
 
     def wl_name(self):

@@ -11,8 +11,8 @@ def test_candidates():
     assert autotune.candidates("fp64", 40) == [128, 256, 512]
     assert autotune.candidates("fp64", 119) == [128, 256, 512]
     assert autotune.candidates("fp64", 120) == []          # inverse in global memory: 256 threads
-    assert autotune.candidates("mixed", 112) == [24, 32, 40, 48]
-    assert autotune.candidates("mixed", 264) == [24, 32, 40]   # nacc 6: at most 40 columns
+    assert autotune.candidates("mixed", 112) == [24, 32, 40]
+    assert autotune.candidates("mixed", 264) == [24, 32, 40]   # 6 accumulators: at most 40 columns
     assert autotune.candidates("mixed", 16) == []
     assert autotune.candidates("mixed", 321) == []
     with pytest.raises(ValueError):
@@ -64,7 +64,7 @@ def test_tile_arguments_are_checked(built_lib):
     lib = built_lib
     assert lib.wtg_tile_set(0, 40, 100) == _lib.WTG_EINVAL           # not 128/256/512
     assert lib.wtg_tile_set(1, 112, 52) == _lib.WTG_EINVAL           # not a multiple of 8
-    assert lib.wtg_tile_set(1, 264, 48) == _lib.WTG_EINVAL           # above 40 at nacc 6
+    assert lib.wtg_tile_set(1, 264, 48) == _lib.WTG_EINVAL           # above 40 columns
     assert lib.wtg_tile_set(1, 400, 32) == _lib.WTG_EINVAL           # beyond the mixed kernel
     assert lib.wtg_tile_set(2, 40, 0) == _lib.WTG_EINVAL
     assert lib.wtg_tile_set(0, 0, 0) == _lib.WTG_EINVAL

@@ -117,7 +117,7 @@ def test_every_tile_gives_the_same_spectrum(models, form, ndim_model):
 
 def test_mixed_engine_with_tuned_widths(models):
     """Engines take the pass widths in force when they are created; widths
-    narrower and wider than the built-in ones give the same batch."""
+    other than the built-in ones (40 columns at both Ndim) give the same batch."""
     ms, gs = models
     tops = [list(range(1, m.nw + 1)) for m in ms]
     bots = [list(range(1, m.nw + 1, 2)) for m in ms]
@@ -127,7 +127,7 @@ def test_mixed_engine_with_tuned_widths(models):
     saved = {m.nw * m.np_: api.get_tile(PREC_MIXED, m.nw * m.np_)[0] for m in ms}
     try:
         api.set_tile(PREC_MIXED, 40, 24)
-        api.set_tile(PREC_MIXED, 112, 48)
+        api.set_tile(PREC_MIXED, 112, 32)
         with api.Engine(gs, tops, bots, precision=PREC_MIXED, max_points=64) as e:
             got = e.run(pm, k, om, eta)
         _close(got, ref)

@@ -5,8 +5,8 @@ The tunable shape is, per Ndim,
 * FP64 (per-model kernel, Ndim <= 119 where the inverse runs in shared memory):
   threads per CTA, 128, 256 or 512 (the GEMM's register rows per pass follow);
 * mixed (split-BF16 products on the tensor cores): the output-column pass width,
-  a multiple of 8 up to the tensor-memory limit (48 columns for Ndim <= 256, 40
-  above), i.e. how many passes of 2 x nacc accumulators cover the product.
+  a multiple of 8 up to the tensor-memory limit (40 columns: 2 x 6 accumulators
+  of w columns in 512), i.e. how many passes of 2 x nacc accumulators cover the product.
 
 ``tune`` times every candidate on a seeded synthetic model of that Ndim through
 the public call (``Model.surface_spectrum``, host buffers in and out), checks that
@@ -42,8 +42,8 @@ def candidates(form: str, ndim: int) -> list[int]:
     if form == "mixed":
         if not 1 <= ndim <= MIXED_MAX_N:
             return []
-        wmax = 40 if ndim > 256 else 48
-        npad = (ndim + 15) // 16 * 16
+        wmax = 40
+        npad = (ndim + 7) // 8 * 8
         # passes narrower than 24 columns regenerate the left factor's digits too often;
         # a pass wider than the padded product adds nothing
         return [w for w in range(24, wmax + 1, 8) if w <= npad]

@@ -2,23 +2,24 @@
 //
 // Every complex product of surfgreen_1985 (src/surfgreen.f90:92-116, zgemm at
 // src/mat_mul.f90:23) runs as an exactly-split BF16 product on tcgen05:
-//   * each FP64 operand is written as 49-bit fixed point against a shared
-//     exponent per row (left factor) or per column (right factor) and cut into
-//     seven 7-bit digits; a digit is an exact BF16 value (with a power-of-two
+//   * each FP64 operand is written as 49-bit fixed point (rounded to nearest)
+//     against a shared exponent per row (left factor) or per column (right
+//     factor) and cut into seven balanced base-128 digits (the leading one in
+//     [0, 128], the others in [-64, 63], so that rounding and truncation errors
+//     have no sign bias); a digit is an exact BF16 value (with a power-of-two
 //     scale folded in), made by one FFMA from the digit's integer bits;
 //   * slice products A^p B^q with p + q <= 8 are issued as BF16 MMAs with FP32
 //     accumulators in tensor memory, one accumulator per slice order
-//     t = p + q for t = 2, 3, 4, 5 (sums of at most 4 * 127^2 * K digit
-//     products stay below 2^24, where the tensor core's accumulation is exact;
-//     above K = 256 order 5 takes two accumulators, one per K half) and one for
-//     t >= 6 (its accumulation truncates; at 2^-28 of the result that costs
-//     ~2^-44);  49 bits are needed because the Newton-Schulz refinement below
-//     can only be as accurate as its residual product;
+//     t = p + q for t = 2 .. 6 (integer terms in the order's unit, exact while
+//     the partial sums stay below 2^24, MxPlan) and one for t = 7, 8 (its
+//     accumulation truncates; at 2^-35 of the result that costs ~2^-51);  49
+//     bits are needed because the Newton-Schulz refinement below can only be
+//     as accurate as its residual product;
 //   * the accumulators are read back (tcgen05.ld), converted to integers and
 //     summed in int64, and the FP64 result is assembled with integer
 //     operations (no FP64 arithmetic for the product itself).
 // The complex product runs in passes over row blocks of 128 (the MMA's M) and
-// column blocks of w <= 48 (40 above Ndim 256): the B digit planes are stored
+// column blocks of w <= 40: the B digit planes are stored
 // as -Yi, Yr, Yi, so that per slice pair two MMAs of N = 2w, Xr [Yr; Yi] and
 // Xi [-Yi; Yr], accumulate [Cr | Ci] = [Xr Yr - Xi Yi | Xr Yi + Xi Yr]; both
 // components share one generation of the A planes and every MMA is twice as
@@ -69,30 +70,42 @@ constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident c
 // M = 128.  Each pass holds nacc FP32 accumulators of 2w columns (both
 // components side by side), so 512 tensor-memory columns bound 2 nacc w;
 // output columns [0, NP) go in ncb blocks of w0 (a multiple of 8; the last
-// block narrower).  nacc = 5 keeps slice orders 2..5 exact for K <= 256; above
-// that order 5 is split over two K halves (nacc = 6), since 4 * 127^2 * K must
-// stay below 2^24.
+// block narrower).  A 7-digit product keeps one accumulator for each slice
+// order t = 2..6, whose terms are integers in the order's own unit, and one
+// for the orders 7 and 8 (nacc = 6).  An accumulator of integer terms adds
+// exactly while its partial sums stay below 2^24.  With the leading digit in
+// [0, 128] and the others in [-64, 63] (balanced digits), order t gathers
+// 2 (t - 1) K digit products (two MMAs a slice pair, one per input component)
+// of at most 2^14 (1, 1), 2^13 (1, q) or 2^12: at most 57344 K for order 6,
+// 49152 K for order 5, so every exact order stays below 2^24 for K <= 292 even
+// with every product at its bound and of one sign (orders <= 5 up to K = 341),
+// and expected partial sums of random digits are a few 10^4.  Terms of
+// different orders in one accumulator are not integers in a common unit and
+// the tensor core's FP32 accumulation truncates them: the orders 7 and 8 share
+// the last accumulator, whose truncation costs about 2^-51 of the result
+// (2^-44 when order 6 shared it as well).
 struct MxPlan {
   int N, NP, nrb, nacc, ncb, w0;
   int wb;                    // B-plane width of the shared-memory layout
-  int split5;                // order 5 summed in two accumulators, one per K half (K > 256)
-  int lumped;                // the last accumulator sums the orders >= 6 (7-digit products)
+  int lumped;                // the last accumulator sums the orders 7 and 8 (7-digit products)
 };
 
-// widest pass: both components side by side, 2 x nacc accumulators of w columns
-// in the 512 tensor-memory columns
-__host__ __device__ inline int mx_wmax(int N) { return (512 / (2 * (N > 256 ? 6 : 5))) & ~7; }
+// accumulators of a 7-digit product: orders 2 .. MX_NACC exact, the rest lumped
+constexpr int MX_NACC = 6;
+
+// widest pass: both components side by side, 2 x MX_NACC accumulators of w
+// columns in the 512 tensor-memory columns
+__host__ __device__ inline int mx_wmax(int) { return (512 / (2 * MX_NACC)) & ~7; }
 
 // The plan of a 4-digit product (28-bit operands, slice pairs p + q <= 5, every
-// order exact: accumulators for orders 2..5, order 5 split over K halves above
-// K = 256, nothing lumped), used where the product only corrects a value whose
-// size it is small against (the Newton-Schulz update G + G R, |R| << 1).  Its
-// passes are as wide as the tensor memory and the layout's B area (3 NSL wb
-// columns of B planes per buffer) allow.
+// order exact: accumulators for orders 2..5, nothing lumped), used where the
+// product only corrects a value whose size it is small against (the
+// Newton-Schulz update G + G R, |R| << 1).  Its passes are as wide as the
+// tensor memory and the layout's B area (3 NSL wb columns of B planes per
+// buffer) allow.
 __host__ __device__ inline MxPlan mx_plan4(const MxPlan& p7) {
   MxPlan p = p7;
-  p.nacc = p7.N > 256 ? 5 : 4;
-  p.split5 = p7.N > 256;
+  p.nacc = 4;
   p.lumped = 0;
   int wmax = (512 / (2 * p.nacc)) & ~7;
   const int bcap = ((3 * NSL * p7.wb) / (3 * 4)) & ~7;
@@ -108,10 +121,9 @@ __host__ __device__ inline MxPlan mx_plan4(const MxPlan& p7) {
 __host__ __device__ inline MxPlan mx_plan(int N, int w0_req = 0) {
   MxPlan p;
   p.N = N;
-  p.NP = (N + 15) & ~15;
+  p.NP = (N + 7) & ~7;          // an MMA's N (2w, both components) needs w a multiple of 8 only
   p.nrb = (N + 127) / 128;
-  p.nacc = N > 256 ? 6 : 5;
-  p.split5 = N > 256;
+  p.nacc = MX_NACC;
   p.lumped = 1;
   const int wmax = mx_wmax(N);
   if (w0_req >= 8 && w0_req <= wmax && (w0_req & 7) == 0) {
@@ -210,7 +222,8 @@ __device__ __forceinline__ int bexp(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
-// |x| as 49-bit fixed point against biased exponent E (|x| < 2^(E-1022))
+// |x| as 49-bit fixed point against biased exponent E (|x| < 2^(E-1022)),
+// rounded to nearest (ties up): at most 2^49
 __device__ __forceinline__ unsigned long long fixed49(double x, int E, unsigned& neg) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   neg = (unsigned)(u >> 63);
@@ -218,9 +231,13 @@ __device__ __forceinline__ unsigned long long fixed49(double x, int E, unsigned&
   unsigned long long m = u & 0xFFFFFFFFFFFFFull;
   if (ex) m |= 1ull << 52;
   else ex = 1;
-  const int sh = E - ex + 4;
-  return sh < 64 ? (m >> sh) : 0ull;
+  const int sh = E - ex + 4;          // >= 4: E is the maximum exponent of the row or column
+  return sh < 64 ? ((m + (1ull << (sh - 1))) >> sh) : 0ull;
 }
+
+// 64 in every 7-bit digit position: f + DIGIT_BIAS has digits g_p in [0, 127]
+// below the leading one, and f = sum (g_p - 64) 128^(7-p) (balanced digits)
+constexpr unsigned long long DIGIT_BIAS = 0x1020408102040ull;
 
 // integer value of an integer-valued float, divided by 2^7 (truncating)
 __device__ __forceinline__ long long f2ll_bits(uint32_t w) {
@@ -419,20 +436,23 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
   __syncthreads();
 }
 
-// BF16x2 bits of (d0 * 2^s, d1 * 2^s) for 7-bit digits, signs in sgn (bits 15
-// and 31).  (2^23 + d) * 2^s - 2^(23+s) by one FFMA is d * 2^s exactly, and
-// its low 16 bits are zero, so the BF16 value is the float's upper half.
-__device__ __forceinline__ uint32_t dig2f(uint32_t d0, uint32_t d1, float sc, float off,
+// BF16x2 bits of ((g0 - 64) * 2^s, (g1 - 64) * 2^s) for biased digits g in
+// [0, 192], element signs in sgn (bits 15 and 31).  (2^23 + g) * 2^s -
+// (2^23 + 64) * 2^s by one FFMA is (g - 64) * 2^s exactly, an integer of at
+// most 8 significant bits times a power of two, so the BF16 value is the
+// float's upper half; the element's sign flips the digit's own.
+__device__ __forceinline__ uint32_t dig2f(uint32_t g0, uint32_t g1, float sc, float off,
                                           uint32_t sgn) {
-  const float f0 = __fmaf_rn(__uint_as_float(0x4B000000u | d0), sc, off);
-  const float f1 = __fmaf_rn(__uint_as_float(0x4B000000u | d1), sc, off);
-  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632) | sgn;
+  const float f0 = __fmaf_rn(__uint_as_float(0x4B000000u | g0), sc, off);
+  const float f1 = __fmaf_rn(__uint_as_float(0x4B000000u | g1), sc, off);
+  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632) ^ sgn;
 }
 
-// digit p (1 = most significant) of a 49-bit value split as hi = bits 21..48, lo = bits 0..20
+// biased digit p (1 = most significant) of g = f + DIGIT_BIAS split as hi =
+// bits 21.., lo = bits 0..20; the leading digit keeps every bit above 42 (g < 2^50)
 template <int P>
 __device__ __forceinline__ uint32_t digit7(uint32_t hi, uint32_t lo) {
-  return P <= 4 ? (hi >> (7 * (4 - P))) & 127u : (lo >> (7 * (7 - P))) & 127u;
+  return P == 1 ? hi >> 21 : P <= 4 ? (hi >> (7 * (4 - P))) & 127u : (lo >> (7 * (7 - P))) & 127u;
 }
 
 // 2^e as a float constant
@@ -441,18 +461,24 @@ __host__ __device__ constexpr float pow2f(int e) {
 }
 
 // the D (7 or 4) leading digit planes (real and imaginary) of one element
-// pair, stored at dst + plane * pstride (words); scale 2^(7 (e0 - p)) for plane p
+// pair, stored at dst + plane * pstride (words); scale 2^(7 (e0 - p)) for plane
+// p.  The digits are balanced (the leading one in [0, 128], the others in
+// [-64, 63]); D = 4 keeps the four leading ones, the operand rounded to 28 bits.
 template <int E0, int D>
 __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned long long fr0,
                                            unsigned long long fr1, unsigned long long fi0,
                                            unsigned long long fi1, uint32_t sr, uint32_t si) {
+  fr0 += DIGIT_BIAS;
+  fr1 += DIGIT_BIAS;
+  fi0 += DIGIT_BIAS;
+  fi1 += DIGIT_BIAS;
   const uint32_t hr0 = (uint32_t)(fr0 >> 21), lr0 = (uint32_t)fr0 & 0x1FFFFFu;
   const uint32_t hr1 = (uint32_t)(fr1 >> 21), lr1 = (uint32_t)fr1 & 0x1FFFFFu;
   const uint32_t hi0 = (uint32_t)(fi0 >> 21), li0 = (uint32_t)fi0 & 0x1FFFFFu;
   const uint32_t hi1 = (uint32_t)(fi1 >> 21), li1 = (uint32_t)fi1 & 0x1FFFFFu;
 #define WTG_PUT(P)                                                                          \
   {                                                                                          \
-    constexpr float sc = pow2f(7 * (E0 - P)), off = -pow2f(23 + 7 * (E0 - P));              \
+    constexpr float sc = pow2f(7 * (E0 - P)), off = -(8388608.0f + 64.0f) * sc;             \
     dst[(2 * (P - 1)) * pstride] =                                                           \
         dig2f(digit7<P>(hr0, lr0), digit7<P>(hr1, lr1), sc, off, sr);                        \
     dst[(2 * (P - 1) + 1) * pstride] =                                                       \
@@ -467,18 +493,23 @@ __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned 
 
 // the B digit planes of one element pair: per digit q the planes -Yi, Yr, Yi
 // (3(q-1), +1, +2), so that [Yr; Yi] and [-Yi; Yr] are each one operand of 2w
-// rows; -Yi is Yi with both BF16 sign bits flipped.  D leading digits (7 or 4).
+// rows; -Yi is Yi with both BF16 sign bits flipped.  D leading balanced digits
+// (7 or 4), as put_digits.
 template <int D>
 __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigned long long fr0,
                                              unsigned long long fr1, unsigned long long fi0,
                                              unsigned long long fi1, uint32_t sr, uint32_t si) {
+  fr0 += DIGIT_BIAS;
+  fr1 += DIGIT_BIAS;
+  fi0 += DIGIT_BIAS;
+  fi1 += DIGIT_BIAS;
   const uint32_t hr0 = (uint32_t)(fr0 >> 21), lr0 = (uint32_t)fr0 & 0x1FFFFFu;
   const uint32_t hr1 = (uint32_t)(fr1 >> 21), lr1 = (uint32_t)fr1 & 0x1FFFFFu;
   const uint32_t hi0 = (uint32_t)(fi0 >> 21), li0 = (uint32_t)fi0 & 0x1FFFFFu;
   const uint32_t hi1 = (uint32_t)(fi1 >> 21), li1 = (uint32_t)fi1 & 0x1FFFFFu;
 #define WTG_PUTB(P)                                                                         \
   {                                                                                          \
-    constexpr float sc = pow2f(7 * (5 - P)), off = -pow2f(23 + 7 * (5 - P));               \
+    constexpr float sc = pow2f(7 * (5 - P)), off = -(8388608.0f + 64.0f) * sc;              \
     const uint32_t br = dig2f(digit7<P>(hr0, lr0), digit7<P>(hr1, lr1), sc, off, sr);       \
     const uint32_t bi = dig2f(digit7<P>(hi0, li0), digit7<P>(hi1, li1), sc, off, si);       \
     dst[(3 * (P - 1)) * pstride] = bi ^ 0x80008000u;                                         \
@@ -551,13 +582,13 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 // address field holds (address >> 4) in its low 14 bits, so a plane offset is
 // added to a base descriptor directly.  Both components in two MMAs of N = 2w
 // per slice pair: Xr [Yr; Yi] and Xi [-Yi; Yr] accumulate [Cr | Ci].  Slice
-// order t = p + q goes to accumulator t - 2 for t <= 5 (with nacc = 6, order 5
-// of the second K half to accumulator 4) and to the last accumulator for
-// t >= 6; accumulator a sits at tensor-memory column 2 w a.  amask holds the
-// accumulators already written in this pass: the first MMA into one overwrites.
-// D digits: slice pairs p + q <= D + 1.
+// order t = p + q goes to accumulator t - 2 while that is one of the nexact
+// exact ones and to the last (lumped) accumulator above; accumulator a sits at
+// tensor-memory column 2 w a.
+// amask holds the accumulators already written in this pass: the first MMA
+// into one overwrites.  D digits: slice pairs p + q <= D + 1.
 template <int D>
-__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int nacc, int khalf,
+__device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int nacc, int nexact,
                          uint32_t& amask) {
   const uint32_t A = saddr(s.buf[b]);
   const uint32_t B = A + 2 * NSL * APLANE;
@@ -571,7 +602,7 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int
 #pragma unroll 1
     for (int q = 1; q + p <= D + 1; ++q) {
       const int t = p + q;
-      const int a = t <= 4 ? t - 2 : (t == 5 ? 3 + khalf : nacc - 1);
+      const int a = t - 2 < nexact ? t - 2 : nacc - 1;
       const uint32_t d = tmem + (uint32_t)(a * 2 * width);
       const uint64_t bNR = bdesc0 + (uint64_t)(3 * (q - 1)) * bplane16;   // [-Yi; Yr]
       const uint64_t bRI = bNR + bplane16;                                 // [Yr; Yi]
@@ -631,8 +662,7 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
         tc_fence_after();
         if (st.abort) break;
         if (tid == 0) {
-          const int khalf = (pl.split5 && 2 * c >= nch) ? 1 : 0;
-          oz_issue<D>(s, st.tmem, b, width, nacc, khalf, amask);
+          oz_issue<D>(s, st.tmem, b, width, nacc, nacc - pl.lumped, amask);
           mma_commit(&s.mbar[b]);
         }
         st.ncommit[b] += 1;
@@ -692,10 +722,10 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
                 for (int a = 0; a < 6; ++a) {
                   if (a >= nacc) continue;
                   if (pl.lumped && a == nacc - 1) {
-                    S += f2ll_bits(v[a][jj]);               // lumped orders >= 6
+                    S += f2ll_bits(v[a][jj]);               // lumped orders >= 7
                   } else {
                     // exact order t: the value is m 2^(56-7t) with |m| < 2^24
-                    const int t = a <= 3 ? a + 2 : 5;
+                    const int t = a + 2;
                     const float sc = __int_as_float((127 + 7 * t - 56) << 23);
                     S += (long long)__float2int_rz(__uint_as_float(v[a][jj]) * sc) << (49 - 7 * t);
                   }
