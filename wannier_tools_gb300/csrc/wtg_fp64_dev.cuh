@@ -230,24 +230,22 @@ __device__ __forceinline__ long long cabs1_key(double2 v) {
 // columns permuted: inverse(i, j) = sM[i + cols[j]*N].  An exact zero pivot
 // leaves the identity (zgesv + inv do the same, src/inverse.f90:51-55) and
 // returns 1.
-__device__ int gj_invert(const double2* __restrict__ X, double2 w, int N, const Shared& s) {
-  const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
+// Gauss-Jordan of the n x n matrix at sM (leading dimension ld) in place, with
+// partial pivoting (first maximal |re|+|im| in the column, as izamax).  The
+// inverse is left with its columns permuted: inverse(i, j) = sM[i + cols[j]*ld].
+// An exact zero pivot leaves the identity (zgesv + inv do the same,
+// src/inverse.f90:51-55) and returns 1.
+__device__ int gj_core(double2* __restrict__ sM, int n, int ld, const Shared& s) {
+  const int T = blockDim.x, tid = threadIdx.x, nn = n * n;
   const int warp = tid >> 5, lane = tid & 31;
-  double2* sM = s.big;
-  for (int e = tid; e < NN; e += T) {
-    const double2 x = X[e];
-    double2 v = make_double2(-x.x, -x.y);                 // 0 - eps off the diagonal
-    if (e % (N + 1) == 0) v = make_double2(w.x - x.x, w.y - x.y);
-    sM[e] = v;
-  }
   if (tid == 0) s.misc[1] = 0;
   __syncthreads();
-  for (int k = 0; k < N; ++k) {
+  for (int k = 0; k < n; ++k) {
     if (warp == 0) {
       long long best = -1;
-      int bi = N;
-      for (int i = k + lane; i < N; i += 32) {
-        const long long v = cabs1_key(sM[i + k * N]);
+      int bi = n;
+      for (int i = k + lane; i < n; i += 32) {
+        const long long v = cabs1_key(sM[i + k * ld]);
         if (v > best) {
           best = v;
           bi = i;
@@ -264,13 +262,13 @@ __device__ int gj_invert(const double2* __restrict__ X, double2 w, int N, const 
       }
       const int p = bi;
       // column k after the row swap k <-> p (entry k itself is not used)
-      for (int i = lane; i < N; i += 32) s.colbuf[i] = sM[(i == p ? k : i) + k * N];
+      for (int i = lane; i < n; i += 32) s.colbuf[i] = sM[(i == p ? k : i) + k * ld];
       if (lane == 0) {
         s.perm[k] = p;
         if (best == 0) {
           s.misc[1] = 1;
         } else {
-          const double2 pv = sM[p + k * N];
+          const double2 pv = sM[p + k * ld];
           const double inv_d = 1.0 / (pv.x * pv.x + pv.y * pv.y);
           s.recip[0] = make_double2(pv.x * inv_d, -pv.y * inv_d);
         }
@@ -280,37 +278,39 @@ __device__ int gj_invert(const double2* __restrict__ X, double2 w, int N, const 
     if (s.misc[1]) break;
     const int p = s.perm[k];
     const double2 r = s.recip[0];
-    for (int j = tid; j < N; j += T) {
-      const double2 akj = sM[k + j * N];
-      const double2 apj = sM[p + j * N];
-      if (p != k) sM[p + j * N] = akj;
+    for (int j = tid; j < n; j += T) {
+      const double2 akj = sM[k + j * ld];
+      const double2 apj = sM[p + j * ld];
+      if (p != k) sM[p + j * ld] = akj;
       const double2 nk = (j == k) ? r : cmul(apj, r);
-      sM[k + j * N] = nk;
+      sM[k + j * ld] = nk;
       s.rowbuf[j] = nk;
     }
     __syncthreads();
-    for (int e = tid; e < NN; e += T) {
-      const int i = e % N, j = e / N;
+    for (int e = tid; e < nn; e += T) {
+      const int i = e % n, j = e / n;
       if (i != k) {
-        double2 v = (j == k) ? make_double2(0.0, 0.0) : sM[e];
+        double2* a = sM + i + j * ld;
+        double2 v = (j == k) ? make_double2(0.0, 0.0) : *a;
         const double2 f = s.colbuf[i];
         const double2 rk = s.rowbuf[j];
         v.x = fma(-f.x, rk.x, v.x);
         v.x = fma(f.y, rk.y, v.x);
         v.y = fma(-f.x, rk.y, v.y);
         v.y = fma(-f.y, rk.x, v.y);
-        sM[e] = v;
+        *a = v;
       }
     }
     __syncthreads();
   }
   const int singular = s.misc[1];
   if (singular) {
-    for (int e = tid; e < NN; e += T) sM[e] = make_double2(e % (N + 1) == 0 ? 1.0 : 0.0, 0.0);
-    for (int j = tid; j < N; j += T) s.cols[j] = j;
+    for (int e = tid; e < nn; e += T)
+      sM[e % n + (e / n) * ld] = make_double2(e % (n + 1) == 0 ? 1.0 : 0.0, 0.0);
+    for (int j = tid; j < n; j += T) s.cols[j] = j;
   } else if (tid == 0) {
-    for (int j = 0; j < N; ++j) s.cols[j] = j;
-    for (int k = N - 1; k >= 0; --k) {      // undo the row swaps as column swaps
+    for (int j = 0; j < n; ++j) s.cols[j] = j;
+    for (int k = n - 1; k >= 0; --k) {      // undo the row swaps as column swaps
       const int p = s.perm[k];
       const int t = s.cols[k];
       s.cols[k] = s.cols[p];
@@ -319,6 +319,101 @@ __device__ int gj_invert(const double2* __restrict__ X, double2 w, int N, const 
   }
   __syncthreads();
   return singular;
+}
+
+// (w I - X) into the shared N x N area; rev reads X's indices in reverse order
+__device__ void gj_load(const double2* __restrict__ X, double2 w, int N, bool rev, const Shared& s) {
+  const int T = blockDim.x, NN = N * N;
+  for (int e = threadIdx.x; e < NN; e += T) {
+    const int src = rev ? NN - 1 - e : e;      // (N-1-i) + (N-1-j) N
+    const double2 x = X[src];
+    double2 v = make_double2(-x.x, -x.y);                 // 0 - eps off the diagonal
+    if (e % (N + 1) == 0) v = make_double2(w.x - x.x, w.y - x.y);
+    s.big[e] = v;
+  }
+}
+
+// sM := (w I - X)^-1 by in-place Gauss-Jordan in shared memory (gj_core); the
+// inverse is left with its columns permuted: inverse(i, j) = sM[i + cols[j]*N].
+__device__ int gj_invert(const double2* __restrict__ X, double2 w, int N, const Shared& s) {
+  gj_load(X, w, N, false, s);
+  return gj_core(s.big, N, N, s);
+}
+
+// The trailing nb x nb block of (w I - X)^-1, or with rev the leading block
+// (X's indices read in reverse order), in shared memory: Gaussian elimination
+// of the other m = N - nb columns, pivoting among their own rows, leaves the
+// Schur complement of that part in the trailing block, and gj_core inverts it:
+// (N^3 - nb^3) / 3 + nb^3 complex multiply-adds instead of N^3.  The block
+// inverse stays at s.big + m + m N: block(i, j) = s.big[m + i + (m + cols[j]) N].
+// The spectral sums of src/surfstat.f90:149-160 and src/fermiarc.f90:237-248
+// read one principal layer's block of GLL or GRR only.  Returns 1 on an exact
+// zero pivot (the caller then takes the full inverse).
+__device__ int schur_block_invert(const double2* __restrict__ X, double2 w, int N, int nb,
+                                  bool rev, const Shared& s) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;
+  const int m = N - nb;
+  double2* sM = s.big;
+  gj_load(X, w, N, rev, s);
+  if (tid == 0) s.misc[1] = 0;
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    if (warp == 0) {
+      long long best = -1;
+      int bi = m;
+      for (int i = k + lane; i < m; i += 32) {
+        const long long v = cabs1_key(sM[i + k * N]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      const int p = bi;
+      if (best == 0) {
+        if (lane == 0) s.misc[1] = 1;
+      } else {
+        const double2 pv = sM[p + k * N];
+        const double inv_d = 1.0 / (pv.x * pv.x + pv.y * pv.y);
+        const double2 r = make_double2(pv.x * inv_d, -pv.y * inv_d);
+        // multipliers of the rows below k after the swap k <-> p, and the pivot row
+        for (int i = k + 1 + lane; i < N; i += 32)
+          s.colbuf[i] = cmul(sM[(i == p ? k : i) + k * N], r);
+        for (int j = k + 1 + lane; j < N; j += 32) s.rowbuf[j] = sM[p + j * N];
+        if (lane == 0) s.misc[2] = p;
+      }
+    }
+    __syncthreads();
+    if (s.misc[1]) break;
+    const int p = s.misc[2];
+    // trailing update; row p receives what row k held (row k itself is done)
+    for (int j = k + 1 + warp; j < N; j += nwarp) {
+      const double2 rk = s.rowbuf[j];
+      for (int i = k + 1 + lane; i < N; i += 32) {
+        double2 v = sM[(i == p ? k : i) + j * N];
+        const double2 f = s.colbuf[i];
+        v.x = fma(-f.x, rk.x, v.x);
+        v.x = fma(f.y, rk.y, v.x);
+        v.y = fma(-f.x, rk.y, v.y);
+        v.y = fma(-f.y, rk.x, v.y);
+        sM[i + j * N] = v;
+      }
+    }
+    __syncthreads();
+  }
+  if (s.misc[1]) {
+    __syncthreads();
+    return 1;
+  }
+  return gj_core(sM + m + (size_t)m * N, nb, N, s);
 }
 
 constexpr int GJ_ROWS = 10;    // rows per lane of the global-memory inverse: Ndim <= 320

@@ -1341,9 +1341,17 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
   const bool gsm = N <= MX_SMEM_GJ_N;
   const Shared fs = fp64_layout(smem_dyn, N, GJ_PANEL, gsm);
-  // (w - X)^-1 in FP64, optionally stored un-permuted to dst; ginv reads the result
-  auto invert = [&](const double2* X, double2* dst) -> int {
+  // (w - X)^-1 in FP64, optionally stored un-permuted to dst; ginv reads the
+  // result.  blk 1 / 2: only the leading / trailing nw x nw block (one principal
+  // layer), by the Schur complement of the rest (schur_block_invert), where the
+  // spectral sums read nothing else; a zero pivot there takes the full inverse.
+  const int m = N - o.nw;
+  int blk = 0;
+  auto invert = [&](const double2* X, double2* dst, int want_blk) -> int {
     __syncthreads();                  // the area aliases buffers the loop just used
+    blk = (gsm && !dst && m > 0) ? want_blk : 0;
+    if (blk && !schur_block_invert(X, w, N, o.nw, blk == 1, fs)) return 0;
+    blk = 0;
     int sing;
     if (gsm) {
       sing = gj_invert(X, w, N, fs);
@@ -1355,11 +1363,16 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     return sing;
   };
   auto ginv = [&](int i, int j) {
+    if (blk) {                        // block entry (i, j): local indices in the block
+      const int li = blk == 1 ? o.nw - 1 - i : i - m;
+      const int lj = blk == 1 ? o.nw - 1 - j : j - m;
+      return fs.big[m + li + (size_t)(m + fs.cols[lj]) * N];
+    }
     return gsm ? fs.big[i + fs.cols[j] * N] : Mi[i + (size_t)fs.cols[j] * N];
   };
   double dl = 0.0, dr = 0.0, db = 0.0;
   double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  if (invert(ES, gll)) stat |= PT_SINGULAR;                   // :127-128
+  if (invert(ES, gll, 1)) stat |= PT_SINGULAR;                // :127-128
   if (tid == 0) {
     for (int q = 0; q < o.ntop; ++q) {
       const int io = o.top[q] - 1;
@@ -1369,7 +1382,9 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     if (o.spin[0]) spin_sums(ginv, o.nw, o.ntop, o.top, 0, o.divide_by_pi, spin[0], spin[1], spin[2]);
   }
   __syncthreads();
-  if (invert(ET, grr)) stat |= PT_SINGULAR;                   // :130-131
+  // surfstat's spin sums read GRR's leading block as well (src/surfstat.f90:178-192)
+  if (invert(ET, grr, (o.spin[0] && !o.spin_right_bottom) ? 0 : 2))    // :130-131
+    stat |= PT_SINGULAR;
   if (tid == 0) {
     for (int q = 0; q < o.nbot; ++q) {
       const int io = N - o.nw + o.bot[q] - 1;
@@ -1384,7 +1399,7 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     }
   }
   __syncthreads();
-  if (invert(E, gb)) stat |= PT_SINGULAR;                     // :133-134
+  if (invert(E, gb, 0)) stat |= PT_SINGULAR;                  // :133-134
   if (tid == 0) {
     for (int i = 0; i < N; ++i) {
       const double v = ginv(i, i).y;
