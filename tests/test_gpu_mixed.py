@@ -129,6 +129,26 @@ def test_spin_mixed(built_lib):
         assert np.max(np.abs(got[name] - ref[name])) <= 1e-6 * scale, name
 
 
+@pytest.mark.parametrize("arc", [False, True])
+def test_spin_mixed_ndim132(built_lib, arc):
+    """Ndim 132 (Np 3): GLL and GRR come from Schur complements eliminated in
+    global memory (GRR in full where surfstat's spin sums read its top block)."""
+    nw, np_ = 44, 3
+    m = synthetic.make_model(nw, np_, seed=78)
+    kp = synthetic.random_kpoints(2, seed=4)
+    om = np.array([0.05]) * EV
+    top, bot = [1, 2, 5, 23, 40], [1, 3, 24, 44]
+    ref = O.surface_spectrum(m.hmnr, m.irvec, m.ndegen, nw, np_, kp, om, 1e-3 * EV, top, bot,
+                             scale=1.0 / O.PI_REF if arc else 1.0, with_spin=True)
+    with api.Model.from_surface_model(m) as g:
+        got = g.surface_spectrum_spin(kp, om, 1e-3 * EV, top, bot, arc=arc, precision=PREC_MIXED)
+    for name in ("dos_l", "dos_r", "dos_bulk"):
+        assert _rel(got[name], ref[name]) <= 1e-5, name
+    scale = np.abs(ref["dos_l"]).max()
+    for name in ("sx_l", "sy_l", "sz_l", "sx_r", "sy_r", "sz_r"):
+        assert np.max(np.abs(got[name] - ref[name])) <= 1e-5 * scale, name
+
+
 def _oracle_point(args):
     from oracle import wt_oracle as Ow
     from wannier_tools_gb300 import synthetic as S

@@ -416,6 +416,104 @@ __device__ int schur_block_invert(const double2* __restrict__ X, double2 w, int 
   return gj_core(sM + m + (size_t)m * N, nb, N, s);
 }
 
+// Layout of schur_block_invert_global: the nb x nb Schur complement, then the
+// small arrays sized for the full N (the elimination's multipliers and pivot row).
+__host__ __device__ constexpr int schur_area_bytes(int N, int nb) {
+  return nb * nb * 16 + N * 32 + 16 * GJ_PANEL + 32 * 8 + N * 8 + 16;
+}
+__device__ __forceinline__ Shared schur_layout(unsigned char* smraw, int N, int nb) {
+  Shared s;
+  s.big = reinterpret_cast<double2*>(smraw);
+  s.sX = s.sY = s.pan = s.mult = nullptr;
+  s.colbuf = s.big + (size_t)nb * nb;
+  s.rowbuf = s.colbuf + N;
+  s.recip = s.rowbuf + N;
+  s.red = reinterpret_cast<double*>(s.recip + GJ_PANEL);
+  s.perm = reinterpret_cast<int*>(s.red + 32);
+  s.cols = s.perm + N;
+  s.misc = s.cols + N;
+  return s;
+}
+
+// schur_block_invert for an N x N matrix too large for shared memory: the
+// elimination runs on Mg in global memory (a warp per column, its lanes on
+// consecutive rows), then the nb x nb Schur complement is copied into shared
+// memory (schur_layout) and inverted there by gj_core: block(i, j) =
+// s.big[i + cols[j] nb].  Returns 1 on an exact zero pivot.
+__device__ int schur_block_invert_global(const double2* __restrict__ X, double2 w, int N, int nb,
+                                         bool rev, double2* __restrict__ Mg, const Shared& s) {
+  const int T = blockDim.x, tid = threadIdx.x, NN = N * N;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = T >> 5;
+  const int m = N - nb;
+  for (int e = tid; e < NN; e += T) {
+    const double2 x = X[rev ? NN - 1 - e : e];
+    double2 v = make_double2(-x.x, -x.y);
+    if (e % (N + 1) == 0) v = make_double2(w.x - x.x, w.y - x.y);
+    Mg[e] = v;
+  }
+  if (tid == 0) s.misc[1] = 0;
+  __syncthreads();
+  for (int k = 0; k < m; ++k) {
+    if (warp == 0) {
+      long long best = -1;
+      int bi = m;
+      for (int i = k + lane; i < m; i += 32) {
+        const long long v = cabs1_key(Mg[i + (size_t)k * N]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      const int p = bi;
+      if (best == 0) {
+        if (lane == 0) s.misc[1] = 1;
+      } else {
+        const double2 pv = Mg[p + (size_t)k * N];
+        const double inv_d = 1.0 / (pv.x * pv.x + pv.y * pv.y);
+        const double2 r = make_double2(pv.x * inv_d, -pv.y * inv_d);
+        for (int i = k + 1 + lane; i < N; i += 32)
+          s.colbuf[i] = cmul(Mg[(i == p ? k : i) + (size_t)k * N], r);
+        for (int j = k + 1 + lane; j < N; j += 32) s.rowbuf[j] = Mg[p + (size_t)j * N];
+        if (lane == 0) s.misc[2] = p;
+      }
+    }
+    __syncthreads();
+    if (s.misc[1]) break;
+    const int p = s.misc[2];
+    for (int j = k + 1 + warp; j < N; j += nwarp) {
+      const double2 rk = s.rowbuf[j];
+      double2* col = Mg + (size_t)j * N;
+      for (int i = k + 1 + lane; i < N; i += 32) {
+        double2 v = col[i == p ? k : i];
+        const double2 f = s.colbuf[i];
+        v.x = fma(-f.x, rk.x, v.x);
+        v.x = fma(f.y, rk.y, v.x);
+        v.y = fma(-f.x, rk.y, v.y);
+        v.y = fma(-f.y, rk.x, v.y);
+        col[i] = v;
+      }
+    }
+    __syncthreads();
+  }
+  if (s.misc[1]) {
+    __syncthreads();
+    return 1;
+  }
+  for (int e = tid; e < nb * nb; e += T)
+    s.big[e] = Mg[m + e % nb + (size_t)(m + e / nb) * N];
+  __syncthreads();
+  return gj_core(s.big, nb, nb, s);
+}
+
 constexpr int GJ_ROWS = 10;    // rows per lane of the global-memory inverse: Ndim <= 320
 
 // one complex entry of a lane's register column (row = lane + 32 m) by a

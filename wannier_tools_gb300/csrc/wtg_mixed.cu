@@ -1346,11 +1346,17 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
   // layer), by the Schur complement of the rest (schur_block_invert), where the
   // spectral sums read nothing else; a zero pivot there takes the full inverse.
   const int m = N - o.nw;
+  // above MX_SMEM_GJ_N the elimination runs in workspace matrix 8 and the
+  // block's inverse in shared memory, when the block fits the area
+  const bool gblk = !gsm && schur_area_bytes(N, o.nw) <= MX_FP64_AREA;
+  const Shared fb = schur_layout(smem_dyn, N, o.nw);
   int blk = 0;
   auto invert = [&](const double2* X, double2* dst, int want_blk) -> int {
     __syncthreads();                  // the area aliases buffers the loop just used
-    blk = (gsm && !dst && m > 0) ? want_blk : 0;
-    if (blk && !schur_block_invert(X, w, N, o.nw, blk == 1, fs)) return 0;
+    blk = ((gsm || gblk) && !dst && m > 0) ? want_blk : 0;
+    if (blk && !(gsm ? schur_block_invert(X, w, N, o.nw, blk == 1, fs)
+                     : schur_block_invert_global(X, w, N, o.nw, blk == 1, Mi, fb)))
+      return 0;
     blk = 0;
     int sing;
     if (gsm) {
@@ -1366,7 +1372,8 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     if (blk) {                        // block entry (i, j): local indices in the block
       const int li = blk == 1 ? o.nw - 1 - i : i - m;
       const int lj = blk == 1 ? o.nw - 1 - j : j - m;
-      return fs.big[m + li + (size_t)(m + fs.cols[lj]) * N];
+      return gsm ? fs.big[m + li + (size_t)(m + fs.cols[lj]) * N]
+                 : fb.big[li + (size_t)fb.cols[lj] * o.nw];
     }
     return gsm ? fs.big[i + fs.cols[j] * N] : Mi[i + (size_t)fs.cols[j] * N];
   };
