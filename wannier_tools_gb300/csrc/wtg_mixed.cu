@@ -19,11 +19,12 @@
 //     summed in int64, and the FP64 result is assembled with integer
 //     operations (no FP64 arithmetic for the product itself).
 // The complex product runs in passes over row blocks of 128 (the MMA's M) and
-// column blocks of w <= 40: the B digit planes are stored
-// as -Yi, Yr, Yi, so that per slice pair two MMAs of N = 2w, Xr [Yr; Yi] and
-// Xi [-Yi; Yr], accumulate [Cr | Ci] = [Xr Yr - Xi Yi | Xr Yi + Xi Yr]; both
-// components share one generation of the A planes and every MMA is twice as
-// wide (MxPlan).
+// column blocks of w <= 40: the B digit planes are stored in two runs, Yr, Yi
+// and -Yi, Yr per digit, so that per slice pair two MMAs of N = 2w, Xr [Yr; Yi]
+// and Xi [-Yi; Yr], accumulate [Cr | Ci] = [Xr Yr - Xi Yi | Xr Yi + Xi Yr]; both
+// components share one generation of the A planes, and the pairs of one A digit
+// with up to 128 / w consecutive B digits whose orders have consecutive
+// accumulators are one MMA of N = 2wg (oz_issue).
 // Inverses in the loop (zgesv with identity, src/inverse.f90:43-55) are an
 // FP32 Gauss-Jordan (shared memory up to Ndim 112, global memory in panels
 // above) followed by Newton-Schulz refinement X <- X + X (I - M X): the
@@ -101,14 +102,14 @@ __host__ __device__ inline int mx_wmax(int) { return (512 / (2 * MX_NACC)) & ~7;
 // order exact: accumulators for orders 2..5, nothing lumped), used where the
 // product only corrects a value whose size it is small against (the
 // Newton-Schulz update G + G R, |R| << 1).  Its passes are as wide as the
-// tensor memory and the layout's B area (3 NSL wb columns of B planes per
-// buffer) allow.
+// tensor memory and the layout's B area (4 NSL planes of wb rows per buffer)
+// allow.
 __host__ __device__ inline MxPlan mx_plan4(const MxPlan& p7) {
   MxPlan p = p7;
   p.nacc = 4;
   p.lumped = 0;
   int wmax = (512 / (2 * p.nacc)) & ~7;
-  const int bcap = ((3 * NSL * p7.wb) / (3 * 4)) & ~7;
+  const int bcap = ((4 * NSL * p7.wb) / (4 * 4)) & ~7;
   if (bcap < wmax) wmax = bcap;
   p.ncb = (p.NP + wmax - 1) / wmax;
   p.w0 = ((p.NP + p.ncb - 1) / p.ncb + 7) & ~7;
@@ -305,7 +306,7 @@ struct MxShared {
 };
 
 __host__ __device__ __forceinline__ int bufbytes_of(int WB) {
-  return 2 * NSL * APLANE + 3 * NSL * WB * KCH * 2;
+  return 2 * NSL * APLANE + 4 * NSL * WB * KCH * 2;
 }
 
 // Bytes of the FP64 Gauss-Jordan working area of the final inverses
@@ -491,10 +492,11 @@ __device__ __forceinline__ void put_digits(uint32_t* dst, int pstride, unsigned 
 #undef WTG_PUT
 }
 
-// the B digit planes of one element pair: per digit q the planes -Yi, Yr, Yi
-// (3(q-1), +1, +2), so that [Yr; Yi] and [-Yi; Yr] are each one operand of 2w
-// rows; -Yi is Yi with both BF16 sign bits flipped.  D leading balanced digits
-// (7 or 4), as put_digits.
+// the B digit planes of one element pair, in two runs: Yr, Yi of digit q at
+// planes 2(q-1), +1 and -Yi, Yr at 2D + 2(q-1), +1, so that [Yr; Yi] and
+// [-Yi; Yr] of g consecutive digits are each one operand of 2wg rows (oz_issue);
+// -Yi is Yi with both BF16 sign bits flipped.  D leading balanced digits (7 or
+// 4), as put_digits.
 template <int D>
 __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigned long long fr0,
                                              unsigned long long fr1, unsigned long long fi0,
@@ -512,9 +514,10 @@ __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigne
     constexpr float sc = pow2f(7 * (5 - P)), off = -(8388608.0f + 64.0f) * sc;              \
     const uint32_t br = dig2f(digit7<P>(hr0, lr0), digit7<P>(hr1, lr1), sc, off, sr);       \
     const uint32_t bi = dig2f(digit7<P>(hi0, li0), digit7<P>(hi1, li1), sc, off, si);       \
-    dst[(3 * (P - 1)) * pstride] = bi ^ 0x80008000u;                                         \
-    dst[(3 * (P - 1) + 1) * pstride] = br;                                                   \
-    dst[(3 * (P - 1) + 2) * pstride] = bi;                                                   \
+    dst[(2 * (P - 1)) * pstride] = br;                                                       \
+    dst[(2 * (P - 1) + 1) * pstride] = bi;                                                   \
+    dst[(2 * D + 2 * (P - 1)) * pstride] = bi ^ 0x80008000u;                                 \
+    dst[(2 * D + 2 * (P - 1) + 1) * pstride] = br;                                           \
   }
   WTG_PUTB(1) WTG_PUTB(2) WTG_PUTB(3) WTG_PUTB(4)
   if constexpr (D > 4) {
@@ -563,7 +566,7 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     uint32_t* dst = reinterpret_cast<uint32_t*>(B) + it;
     if (j >= N) {                                  // padding columns
 #pragma unroll
-      for (int pl = 0; pl < 3 * D; ++pl) dst[pl * bstride] = 0u;
+      for (int pl = 0; pl < 4 * D; ++pl) dst[pl * bstride] = 0u;
       continue;
     }
     const int F = expB[j];
@@ -580,13 +583,18 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
 
 // all slice-pair MMAs of one chunk (thread 0 only).  The descriptors' start
 // address field holds (address >> 4) in its low 14 bits, so a plane offset is
-// added to a base descriptor directly.  Both components in two MMAs of N = 2w
-// per slice pair: Xr [Yr; Yi] and Xi [-Yi; Yr] accumulate [Cr | Ci].  Slice
+// added to a base descriptor directly.  Both components in two MMAs per group
+// of slice pairs: Xr [Yr; Yi] and Xi [-Yi; Yr] accumulate [Cr | Ci].  Slice
 // order t = p + q goes to accumulator t - 2 while that is one of the nexact
 // exact ones and to the last (lumped) accumulator above; accumulator a sits at
-// tensor-memory column 2 w a.
-// amask holds the accumulators already written in this pass: the first MMA
-// into one overwrites.  D digits: slice pairs p + q <= D + 1.
+// tensor-memory column 2 w a.  For one digit p of X, the pairs of g
+// consecutive digits q whose orders go to g consecutive accumulators are one
+// MMA of N = 2 w g <= 256 over the B planes of those digits (stored side by
+// side, put_digits_b): the A planes are read once for the group.  amask holds
+// the accumulators already written in this pass: the first MMA into one
+// overwrites, so a group takes accumulators that are all new or all written
+// (digit p = 1 reaches every accumulator first).  D digits: slice pairs
+// p + q <= D + 1.
 template <int D>
 __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int nacc, int nexact,
                          uint32_t& amask) {
@@ -594,23 +602,32 @@ __device__ void oz_issue(const MxShared& s, uint32_t tmem, int b, int width, int
   const uint32_t B = A + 2 * NSL * APLANE;
   const uint64_t bplane16 = (uint64_t)width * KCH * 2 >> 4;
   const uint64_t adesc0 = sdesc(A), bdesc0 = sdesc(B);
-  const uint32_t id2 = idesc(2 * width, 0);
+  const int gmax = 128 / width;                  // 2 w g <= 256 columns
 #pragma unroll 1
   for (int p = 1; p <= D; ++p) {
     const uint64_t aR = adesc0 + (uint64_t)(2 * (p - 1)) * (APLANE >> 4);
     const uint64_t aI = aR + (APLANE >> 4);
+    int q = 1;
 #pragma unroll 1
-    for (int q = 1; q + p <= D + 1; ++q) {
-      const int t = p + q;
-      const int a = t - 2 < nexact ? t - 2 : nacc - 1;
-      const uint32_t d = tmem + (uint32_t)(a * 2 * width);
-      const uint64_t bNR = bdesc0 + (uint64_t)(3 * (q - 1)) * bplane16;   // [-Yi; Yr]
-      const uint64_t bRI = bNR + bplane16;                                 // [Yr; Yi]
-      const uint32_t bit = 1u << a;
-      const uint32_t acc = (amask & bit) ? 1u : 0u;
-      amask |= bit;
-      mma_bf16(d, aR, bRI, id2, acc);
-      mma_bf16(d, aI, bNR, id2, 1u);
+    while (q + p <= D + 1) {
+      const int t0 = p + q;
+      const int a0 = t0 - 2 < nexact ? t0 - 2 : nacc - 1;
+      const uint32_t touched = (amask >> a0) & 1u;
+      int g = 1;
+      while (g < gmax && q + g + p <= D + 1) {
+        const int t = t0 + g;
+        const int a = t - 2 < nexact ? t - 2 : nacc - 1;
+        if (a != a0 + g || ((amask >> a) & 1u) != touched) break;
+        ++g;
+      }
+      const uint32_t d = tmem + (uint32_t)(a0 * 2 * width);
+      const uint64_t bRI = bdesc0 + (uint64_t)(2 * (q - 1)) * bplane16;           // [Yr; Yi] ...
+      const uint64_t bNR = bdesc0 + (uint64_t)(2 * D + 2 * (q - 1)) * bplane16;   // [-Yi; Yr] ...
+      const uint32_t id = idesc(2 * width * g, 0);
+      amask |= ((1u << g) - 1u) << a0;
+      mma_bf16(d, aR, bRI, id, touched);
+      mma_bf16(d, aI, bNR, id, 1u);
+      q += g;
     }
   }
 }
