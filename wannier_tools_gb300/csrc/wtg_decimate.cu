@@ -80,7 +80,21 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
   double2* M1 = W + (size_t)6 * NN;
   double2* M2 = W + (size_t)7 * NN;
   // (w - X)^-1, optionally stored un-permuted to dst; ginv reads the result
-  auto invert = [&](const double2* X, double2* dst) -> int {
+  // blk 1 / 2: only the leading / trailing Num_wann block of the inverse (one
+  // principal layer), from the Schur complement of the rest, where the spectral
+  // sums read nothing else (schur_block_invert); a zero pivot there takes the
+  // full inverse.  With GI the block's inverse needs its Num_wann^2 area within
+  // the stage area every launch of this Ndim has (KC = 16).
+  const int m = N - o.nw;
+  const bool gblk = !GI || schur_area_bytes(N, o.nw) <= fp64_gi_smem_bytes(N);
+  const Shared fb = schur_layout(reinterpret_cast<unsigned char*>(s.big), N, o.nw);
+  int blk = 0;
+  auto invert = [&](const double2* X, double2* dst, int want_blk) -> int {
+    blk = (gblk && !dst && m > 0) ? want_blk : 0;
+    if (blk && !(GI ? schur_block_invert_global(X, w, N, o.nw, blk == 1, Mg, fb)
+                    : schur_block_invert(X, w, N, o.nw, blk == 1, s)))
+      return 0;
+    blk = 0;
     int sing;
     if (GI) {
       sing = gj_invert_global(X, w, N, Mg, s);
@@ -92,6 +106,12 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
     return sing;
   };
   auto ginv = [&](int i, int j) {
+    if (blk) {                        // block entry (i, j): local indices in the block
+      const int li = blk == 1 ? o.nw - 1 - i : i - m;
+      const int lj = blk == 1 ? o.nw - 1 - j : j - m;
+      return GI ? fb.big[li + (size_t)fb.cols[lj] * o.nw]
+                : s.big[m + li + (size_t)(m + s.cols[lj]) * N];
+    }
     return GI ? Mg[i + (size_t)s.cols[j] * N] : s.big[i + s.cols[j] * N];
   };
 
@@ -99,7 +119,7 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
   bool conv = false;
   for (int itc = 1; itc <= o.itermax; ++itc) {                // src/surfgreen.f90:86
     it = itc;
-    if (invert(E, G)) st |= PT_SINGULAR;                      // :88-89
+    if (invert(E, G, 0)) st |= PT_SINGULAR;                   // :88-89
     __syncthreads();
     gemm<RP, EPI_STORE, GI>(Al, G, N, KC, s, M1, nullptr);              // :92
     gemm<RP, EPI_STORE, GI>(Be, G, N, KC, s, M2, nullptr);              // :95
@@ -125,7 +145,7 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
   double dl = 0.0, dr = 0.0, db = 0.0;
   double spin[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   // GLL = (w - eps_s)^-1                                     // :127-128
-  if (invert(ES, gll)) st |= PT_SINGULAR;
+  if (invert(ES, gll, 1)) st |= PT_SINGULAR;
   if (tid == 0) {
     for (int q = 0; q < o.ntop; ++q) {
       const int io = o.top[q] - 1;
@@ -137,7 +157,8 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
   }
   __syncthreads();
   // GRR = (w - eps_t)^-1                                     // :130-131
-  if (invert(ET, grr)) st |= PT_SINGULAR;
+  // surfstat's spin sums read GRR's leading block as well (src/surfstat.f90:178-192)
+  if (invert(ET, grr, (o.spin[0] && !o.spin_right_bottom) ? 0 : 2)) st |= PT_SINGULAR;
   if (tid == 0) {
     for (int q = 0; q < o.nbot; ++q) {
       const int io = N - o.nw + o.bot[q] - 1;
@@ -153,7 +174,7 @@ __device__ void fp64_solve(int N, int KC, double2 w, const O& o, double2* gll, d
   }
   __syncthreads();
   // GB = (w - eps)^-1                                        // :133-134
-  if (invert(E, gb)) st |= PT_SINGULAR;
+  if (invert(E, gb, 0)) st |= PT_SINGULAR;
   if (tid == 0) {
     for (int i = 0; i < N; ++i) {
       const double v = ginv(i, i).y;

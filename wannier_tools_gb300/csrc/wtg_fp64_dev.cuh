@@ -416,6 +416,13 @@ __device__ int schur_block_invert(const double2* __restrict__ X, double2 w, int 
   return gj_core(sM + m + (size_t)m * N, nb, N, s);
 }
 
+// dynamic shared memory of an FP64 decimation launch whose inverse runs in
+// global memory (two GEMM stages of N x 16, then the small arrays): the same for
+// the per-model and the batch kernels at this Ndim
+__host__ __device__ constexpr int fp64_gi_smem_bytes(int N) {
+  return 2 * N * 16 * 16 + N * 32 + 16 * GJ_PANEL + 32 * 8 + N * 8 + 16;
+}
+
 // Layout of schur_block_invert_global: the nb x nb Schur complement, then the
 // small arrays sized for the full N (the elimination's multipliers and pivot row).
 __host__ __device__ constexpr int schur_area_bytes(int N, int nb) {
