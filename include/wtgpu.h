@@ -59,12 +59,13 @@ extern "C" {
 /* precision modes */
 #define WTG_PREC_FP64  0        /* all-FP64 decimation (FP64 DFMA pipe); Ndim <= 320 (above
                                    119 the inverse runs in global memory) */
-#define WTG_PREC_MIXED 1        /* products as exact BF16 digit splits on the tcgen05 tensor
-                                   cores (49-bit operands, FP32 accumulation exact per slice
-                                   order, int64 recombination); in-loop inverses FP32
-                                   Gauss-Jordan + Newton-Schulz refinement on those products;
-                                   the final GLL / GRR / GB inverses and the convergence norm
-                                   in FP64; Ndim <= 320 */
+#define WTG_PREC_MIXED 1        /* products as BF16 digit splits on the tcgen05 tensor cores
+                                   (49-bit rounded operands in balanced 7-bit digits, FP32
+                                   accumulation exact per slice order up to 6, int64
+                                   recombination); in-loop inverses FP32 Gauss-Jordan +
+                                   Newton-Schulz refinement on those products; the final
+                                   GLL / GRR / GB inverses and the convergence norm in FP64;
+                                   Ndim <= 320 */
 
 typedef struct wtg_model* wtg_model_t;
 
@@ -346,7 +347,7 @@ int wtg_engine_graph_info(wtg_engine_t engine, int* graphs, long long* graph_lau
  *   WTG_PREC_FP64   value = threads per CTA of the per-model FP64 kernel, 128, 256
  *                   or 512 (Ndim above the shared-memory inverse always uses 256)
  *   WTG_PREC_MIXED  value = output-column pass width of the split-BF16 products, a
- *                   multiple of 8 up to 48 (Ndim <= 256) or 40 (above)
+ *                   multiple of 8 up to 40
  * value 0 restores the built-in choice.  Results do not depend on the tile beyond
  * the order of the convergence norm's block sum (every output element is summed in
  * the same order; spectra agree to 1e-12).  Set tiles before creating engines
