@@ -72,7 +72,7 @@ def test_inverse_near_pole(built_lib):
     a = w * np.eye(40) - h00
     ref = np.linalg.inv(a)
     gmx, st = api.inv(a, PREC_MIXED)
-    # split products good to ~2^-44 normwise: error ~ 1e-12 x condition number (~1e6 here)
+    # split products good to ~1e-14 normwise: error well below 1e-12 x condition number (~1e6 here)
     assert st == 0 and nrel(gmx, ref) <= 1e-12 * np.linalg.cond(a)
 
 

@@ -84,7 +84,7 @@ constexpr int MX_ROWS = MX_MAXN / 32;  // rows per lane of a register-resident c
 // different orders in one accumulator are not integers in a common unit and
 // the tensor core's FP32 accumulation truncates them: the orders 7 and 8 share
 // the last accumulator, whose truncation costs about 2^-51 of the result
-// (2^-44 when order 6 shared it as well).
+// (sharing it with order 6 as well costs about 2^-44).
 struct MxPlan {
   int N, NP, nrb, nacc, ncb, w0;
   int wb;                    // B-plane width of the shared-memory layout
