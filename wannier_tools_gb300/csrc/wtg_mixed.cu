@@ -388,7 +388,8 @@ __device__ __forceinline__ void buffer_ready(MxShared& s, MxState& st, int b) {
 // A part whose flag is off keeps what the previous product left (the same
 // operand on the same side).
 __device__ void oz_exponents(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
-                             MxShared& s, bool rows, bool cols) {
+                             MxShared& s, bool rows, bool cols, const double2* __restrict__ Xlo = nullptr) {
+  const int M = Xlo ? 2 * N : N;         // rows N.. of a row-stacked product come from Xlo
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   if (rows) {
   for (int r = threadIdx.x; r < MX_MAXN; r += blockDim.x) s.expA[r] = 0;
@@ -398,22 +399,22 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
   for (int m = 0; m < MX_ROWS; ++m) rmax[m] = 0;
   // two columns of X per step so that twice the loads are in flight
   for (int k = warp; k < N; k += 2 * nwarp) {
-    const double2* xc0 = X + (size_t)k * N;
-    const double2* xc1 = X + (size_t)min(k + nwarp, N - 1) * N;
+    const size_t c0 = (size_t)k * N, c1 = (size_t)min(k + nwarp, N - 1) * N;
     const bool two = k + nwarp < N;
 #pragma unroll
     for (int m = 0; m < MX_ROWS; ++m) {
       const int i = lane + 32 * m;
-      if (i < N) {
-        const double2 v0 = xc0[i];
-        const double2 v1 = two ? xc1[i] : v0;
+      if (i < M) {
+        const double2* xr = i < N ? X + i : Xlo + (i - N);
+        const double2 v0 = xr[c0];
+        const double2 v1 = two ? xr[c1] : v0;
         rmax[m] = max(rmax[m], max(max(bexp(v0.x), bexp(v0.y)), max(bexp(v1.x), bexp(v1.y))));
       }
     }
   }
 #pragma unroll
   for (int m = 0; m < MX_ROWS; ++m)
-    if (lane + 32 * m < N) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
+    if (lane + 32 * m < M) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
   }
   if (cols)
   for (int j = warp; j < N; j += 2 * nwarp) {
@@ -535,7 +536,8 @@ __device__ __forceinline__ void put_digits_b(uint32_t* dst, int pstride, unsigne
 template <int D>
 __device__ void oz_generate(const double2* __restrict__ X, const double2* __restrict__ Y, int N,
                             int WB, int k0, int rb0, int jb, int width, const MxShared& s, int b,
-                            int gtid, int gthreads) {
+                            int gtid, int gthreads, const double2* __restrict__ Xlo) {
+  const int M = Xlo ? 2 * N : N;         // rows N.. of a row-stacked product come from Xlo
   unsigned char* __restrict__ A = shm(s, s.buf[b]);
   unsigned char* __restrict__ B = A + 2 * NSL * APLANE;
   const int* __restrict__ expA = shm(s, s.expA);
@@ -545,15 +547,16 @@ __device__ void oz_generate(const double2* __restrict__ X, const double2* __rest
     const int cm = it >> 5, ln = it & 31;
     const int il = (cm >> 1) * 8 + (ln >> 2), kk = (cm & 1) * 8 + (ln & 3) * 2, i = rb0 + il;
     uint32_t* dst = reinterpret_cast<uint32_t*>(A) + it;
-    if (i >= N) {                                  // padding rows of the M = 128 tile
+    if (i >= M) {                                  // padding rows of the M = 128 tile
 #pragma unroll
       for (int pl = 0; pl < 2 * D; ++pl) dst[pl * (APLANE / 4)] = 0u;
       continue;
     }
     const int E = expA[i];
+    const double2* xr = i < N ? X + i : Xlo + (i - N);
     double2 x0 = make_double2(0.0, 0.0), x1 = x0;
-    if (k0 + kk < N) x0 = X[i + (size_t)(k0 + kk) * N];
-    if (k0 + kk + 1 < N) x1 = X[i + (size_t)(k0 + kk + 1) * N];
+    if (k0 + kk < N) x0 = xr[(size_t)(k0 + kk) * N];
+    if (k0 + kk + 1 < N) x1 = xr[(size_t)(k0 + kk + 1) * N];
     unsigned n0r, n0i, n1r, n1i;
     const unsigned long long f0r = fixed49(x0.x, E, n0r), f0i = fixed49(x0.y, E, n0i);
     const unsigned long long f1r = fixed49(x1.x, E, n1r), f1i = fixed49(x1.y, E, n1i);
@@ -647,17 +650,31 @@ __device__ __forceinline__ double cabs64(double re, double im) {
 // REUSE bit 0: X is the previous product's X (its row exponents are in expA);
 // bit 1: Y is the previous product's Y (column exponents in expB).
 constexpr int REUSE_X = 1, REUSE_Y = 2;
-template <int EPI, int D = NSL>
+
+// Rows N .. 2N-1 of a row-stacked product (2 Ndim <= 128): X' Y with its own
+// left factor, epilogue (EPI2 of oz_gemm) and outputs, in the same M = 128
+// tile as the first product's rows.  Each output element sees the same digits
+// and the same MMA sums as in a product of its own.
+struct OzLower {
+  const double2* X;
+  double2* out0;
+  double2* out1;
+  const double2* src;
+};
+
+template <int EPI, int EPI2 = -1, int D = NSL>
 __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restrict__ Y,
                           const MxPlan& pl, double2* out0, double2* out1, const double2* src,
-                          MxShared& s, MxState& st, int reuse = 0) {
+                          MxShared& s, MxState& st, int reuse = 0, OzLower lo = OzLower{}) {
   const int N = pl.N, tid = threadIdx.x;
+  const bool stacked = EPI2 >= 0;
+  const int M = stacked ? 2 * N : N;       // rows of the tile that hold outputs
   const int nch = (N + KCH - 1) / KCH;
   const int nacc = pl.nacc, WB = pl.wb;
   const int npass = pl.ncb;
   float nrm = 0.f;
   double nrm_d = 0.0;
-  oz_exponents(X, Y, N, s, !(reuse & REUSE_X), !(reuse & REUSE_Y));
+  oz_exponents(X, Y, N, s, !(reuse & REUSE_X), !(reuse & REUSE_Y), stacked ? lo.X : nullptr);
   __syncthreads();
   for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
     const int rb0 = rb * 128;
@@ -671,7 +688,8 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
         if (tid >= 32) {     // warps 1.. generate while warp 0 issues the previous chunk
           buffer_ready(s, st, b);
           if (!st.abort)
-            oz_generate<D>(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32);
+            oz_generate<D>(X, Y, N, WB, c * KCH, rb0, jb, width, s, b, tid - 32, blockDim.x - 32,
+                           stacked ? lo.X : nullptr);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
@@ -701,8 +719,15 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
         const int row = rb0 + quad * 32 + lane;
         // a warp whose 32 tensor-memory lanes are all padding rows has nothing to drain
         const int nhw = blockDim.x >> 7;
-        const int cb = hw * 4, ce = rb0 + quad * 32 < N ? width : 0;
-        const int er = row < N ? expA[row] : 0;
+        const int cb = hw * 4, ce = rb0 + quad * 32 < M ? width : 0;
+        const int er = row < M ? expA[row] : 0;
+        // the lower rows of a stacked product: their own epilogue and outputs
+        const bool upper = !stacked || row < N;
+        const int epi = upper ? EPI : EPI2;
+        const int rowL = upper ? row : row - N;
+        double2* const o0b = upper ? out0 : lo.out0;
+        double2* const o1b = upper ? out1 : lo.out1;
+        const double2* const srcb = upper ? src : lo.src;
         const uint32_t bank = (uint32_t)(comp * width);
         for (int c0 = cb; c0 < ce; c0 += 4 * nhw) {
           uint32_t v[6][4];
@@ -711,22 +736,22 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
           for (int a = 0; a < 6; ++a)
             if (a < nacc) tmem_ld4(ta + (uint32_t)(a * 2 * width), v[a]);
           tmem_wait_ld();
-          if (row < N) {
+          if (row < M) {
             double old0[4], old1[4];
 #pragma unroll
             for (int jj = 0; jj < 4; ++jj) {            // the epilogue's loads first
               const int j = jb + c0 + jj;
-              const size_t idx = (size_t)row + (size_t)j * N;
+              const size_t idx = (size_t)rowL + (size_t)j * N;
               old0[jj] = 0.0;
               old1[jj] = 0.0;
               if (j < N) {
-                if (EPI == OZ_ADD2) {
-                  old0[jj] = reinterpret_cast<const double*>(out0 + idx)[comp];
-                  old1[jj] = reinterpret_cast<const double*>(out1 + idx)[comp];
-                } else if (EPI == OZ_ADDTO) {
-                  old0[jj] = reinterpret_cast<const double*>(src + idx)[comp];
-                } else if ((EPI == OZ_STORE_NORM || EPI == OZ_IMINUS) && comp == 1) {
-                  old0[jj] = out0[idx].x;
+                if (epi == OZ_ADD2) {
+                  old0[jj] = reinterpret_cast<const double*>(o0b + idx)[comp];
+                  old1[jj] = reinterpret_cast<const double*>(o1b + idx)[comp];
+                } else if (epi == OZ_ADDTO) {
+                  old0[jj] = reinterpret_cast<const double*>(srcb + idx)[comp];
+                } else if ((epi == OZ_STORE_NORM || epi == OZ_IMINUS) && comp == 1) {
+                  old0[jj] = o0b[idx].x;
                 }
               }
             }
@@ -748,19 +773,19 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
                   }
                 }
                 const double val = assemble(S, er + expB[j] - 1070);
-                const size_t idx = (size_t)row + (size_t)j * N;
-                double* o0 = reinterpret_cast<double*>(out0 + idx) + comp;
-                if (EPI == OZ_STORE) {
+                const size_t idx = (size_t)rowL + (size_t)j * N;
+                double* o0 = reinterpret_cast<double*>(o0b + idx) + comp;
+                if (epi == OZ_STORE) {
                   *o0 = val;
-                } else if (EPI == OZ_ADD2) {
+                } else if (epi == OZ_ADD2) {
                   *o0 = old0[jj] + val;
-                  *(reinterpret_cast<double*>(out1 + idx) + comp) = old1[jj] + val;
-                } else if (EPI == OZ_STORE_NORM) {
+                  *(reinterpret_cast<double*>(o1b + idx) + comp) = old1[jj] + val;
+                } else if (epi == OZ_STORE_NORM) {
                   *o0 = val;
                   if (comp == 1) nrm_d += cabs64(old0[jj], val);   // |alpha_ij| in FP64
-                } else if (EPI == OZ_IMINUS) {
+                } else if (epi == OZ_IMINUS) {
                   double w = -val;
-                  if (comp == 0 && row == j) w += 1.0;
+                  if (comp == 0 && rowL == j) w += 1.0;
                   *o0 = w;
                   if (comp == 1) nrm += fabsf(d2f_bits(old0[jj])) + fabsf(d2f_bits(w));
                 } else {   // OZ_ADDTO
@@ -776,7 +801,7 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
       tc_fence_after();
     }
   }
-  return EPI == OZ_STORE_NORM ? nrm_d : (double)nrm;
+  return (EPI == OZ_STORE_NORM || EPI2 == OZ_STORE_NORM) ? nrm_d : (double)nrm;
 }
 
 __device__ float block_sum_f(float v, MxShared& s) {
@@ -1253,7 +1278,7 @@ __device__ int mixed_inverse(const double2* X, double2 w, const MxPlan& pl, int 
     const float res = block_sum_f(part, s);
     if (!(res < 0.25f * prev)) break;                 // no longer converging (or NaN)
     // Gn = G + G R: R is small, so 4 digits (28 bits) keep G R far below G's own error
-    oz_gemm<OZ_ADDTO, 4>(*Gp, R, mx_plan4(pl), *Gnp, nullptr, *Gp, s, st);
+    oz_gemm<OZ_ADDTO, -1, 4>(*Gp, R, mx_plan4(pl), *Gnp, nullptr, *Gp, s, st);
     double2* tmp = *Gp;
     *Gp = *Gnp;
     *Gnp = tmp;
@@ -1333,14 +1358,25 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     if (mixed_inverse(E, w, pl, ns_iter, &G, &Gn, Mi, R, s, st, 1e-4f)) stat |= PT_SINGULAR;
     // the reference's six products (:92-116), ordered so that each shares an
     // operand with the one before it and reuses its exponents; eps still
-    // receives M1 beta before M2 alpha
-    oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);                       // :92
-    oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st, REUSE_Y);              // :95
-    oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);                             // :98-102
-    const double part =
-        oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st, REUSE_X);    // :113
-    oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st, REUSE_Y);                    // :107-110
-    oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st, REUSE_X);              // :116
+    // receives M1 beta before M2 alpha.  Up to Ndim 64 the products with a
+    // common right factor share one 128-row tile (rows of the second below
+    // those of the first): three products instead of six.
+    double part;
+    if (2 * N <= 128) {
+      oz_gemm<OZ_STORE, OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st, 0,
+                                  OzLower{Be, M2, nullptr, nullptr});               // :92, :95
+      oz_gemm<OZ_ADD2, OZ_STORE>(M1, Be, pl, E, ES, nullptr, s, st, 0,
+                                 OzLower{M2, R, nullptr, nullptr});                 // :98-102, :116
+      part = oz_gemm<OZ_STORE_NORM, OZ_ADD2>(M1, Al, pl, Gn, nullptr, nullptr, s, st, REUSE_X,
+                                             OzLower{M2, E, ET, nullptr});          // :113, :107-110
+    } else {
+      oz_gemm<OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st);                     // :92
+      oz_gemm<OZ_STORE>(Be, G, pl, M2, nullptr, nullptr, s, st, REUSE_Y);            // :95
+      oz_gemm<OZ_ADD2>(M1, Be, pl, E, ES, nullptr, s, st);                           // :98-102
+      part = oz_gemm<OZ_STORE_NORM>(M1, Al, pl, Gn, nullptr, nullptr, s, st, REUSE_X);  // :113
+      oz_gemm<OZ_ADD2>(M2, Al, pl, E, ET, nullptr, s, st, REUSE_Y);                  // :107-110
+      oz_gemm<OZ_STORE>(M2, Be, pl, R, nullptr, nullptr, s, st, REUSE_X);            // :116
+    }
     double2* t0 = Al;
     Al = Gn;
     Gn = t0;
