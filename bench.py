@@ -87,12 +87,13 @@ WORKLOADS = {
                    desc="serving loop: 8 synthetic models Num_wann 8..150, Np 1..3 (Ndim 8..300), "
                         "Poisson requests of 50-400 (k,omega) points, random omega windows in "
                         "[-1,1] eV, eta log-uniform [1e-3,1e-2] eV"),
-    # the large k-path x omega spectrum: 301 k x 501 omega at Ndim 264; two k points
-    # (1002 solves = 6.6 waves of one solve per SM; one k point, 3.3 waves, left 18 % of the
-    # last wave idle) per step, a strided subset of omegas in the CPU sample
+    # the large k-path x omega spectrum: 301 k x 501 omega at Ndim 264; three k points
+    # (1503 solves = 9.9 waves of one solve per SM) per step: two k points (6.6 waves) left
+    # 41 % of the SMs idle in the last wave, 5 % of the step, which the whole 150 801-solve
+    # configuration does not have; a strided subset of omegas in the CPU sample
     "ss_n264": dict(nw=88, np_=3, seed=2026, nk1=301, nk2=None, omega_ev=None, eta_ev=1e-3,
                     divide_by_pi=False, tol=None, cpu_per_core=1, ref_per_core=1,
-                    omega_range=(-0.5, 0.5), nomega=501, step_k=2, cpu_omegas=6,
+                    omega_range=(-0.5, 0.5), nomega=501, step_k=3, cpu_omegas=6,
                     desc="surfstat k-path x omega, synthetic Num_wann=88 Np=3 (Ndim=264), "
                          "301 k x 501 omega in [-0.5,0.5] eV, eta=1e-3 eV"),
 }
