@@ -218,3 +218,39 @@ def test_spectrum_mixed_hardest_arc_points(built_lib):
         print("hardest arc points", name, e)
         assert e <= 1e-5, (name, e)
     assert np.abs(got["iters"].ravel() - ref["iters"].ravel()).max() <= 1
+
+
+def _whole_configuration(nw, np_, seed, kpts, om, eta, tol, divide_by_pi):
+    m = synthetic.make_model(nw, np_, seed=seed)
+    top = list(range(1, nw + 1))
+    with api.Model.from_surface_model(m) as g:
+        ref = g.surface_spectrum(kpts, om, eta, top, top, tol=tol, divide_by_pi=divide_by_pi,
+                                 precision=PREC_FP64)
+        got = g.surface_spectrum(kpts, om, eta, top, top, tol=tol, divide_by_pi=divide_by_pi,
+                                 precision=PREC_MIXED)
+    assert (ref["status"] == 0).all() and (got["status"] == 0).all()
+    assert np.abs(got["iters"] - ref["iters"]).max() <= 1
+    return {name: _rel(got[name].ravel(), ref[name].ravel()) for name in ("dos_l", "dos_r", "dos_bulk")}
+
+
+def test_mixed_whole_kpath_ndim40(built_lib):
+    """Every point of the Ndim-40 k-path x omega spectrum (101 k x 201 omega in
+    [-1, 1] eV, eta 1e-2 eV, tol 1e-10): the mixed form within 1e-5 of the FP64 form."""
+    kp = api.kpath_slab([((-0.5, 0.0), (0.5, 0.0))], 101)
+    om = np.linspace(-1.0, 1.0, 201) * EV
+    errs = _whole_configuration(20, 2, 2023, kp, om, 1e-2 * EV, 1e-10, False)
+    print("whole Ndim-40 k-path", errs)
+    for name, e in errs.items():
+        assert e <= 1e-5, (name, e)
+
+
+def test_mixed_whole_arc_plane_ndim112(built_lib):
+    """Every point of the 201 x 201 Fermi-arc plane of the Ndim-112 model (omega 0,
+    eta 1e-3 eV, every orbital in both lists, /pi): the mixed form within 1e-5 of the
+    FP64 form (3.6e-6 measured), including the points where two valid FP64
+    evaluations already differ by ~1e-7."""
+    _, _, kall = api.kplane_slab(201, 201, (-0.5, -0.5), (1.0, 0.0), (0.0, 1.0))
+    errs = _whole_configuration(56, 2, 2024, kall, np.array([0.0]), 1e-3 * EV, O.ACCURACY_REF, True)
+    print("whole arc plane", errs)
+    for name, e in errs.items():
+        assert e <= 1e-5, (name, e)
