@@ -297,8 +297,8 @@ struct MxShared {
   float2* recip;
   int* perm;
   int* cols;
-  int* expA;               // [128]
-  int* expB;               // [128]
+  int* expA;               // [2 MX_MAXN] row exponents (rows of a row-stacked product)
+  int* expB;               // [MX_MAXN] column exponents
   float* red;              // [32]
   uint64_t* mbar;          // [2]
   uint32_t* tslot;
@@ -345,8 +345,8 @@ __device__ __forceinline__ MxShared mx_layout(unsigned char* smraw, int WB) {
   s.recip = s.rowbuf + MX_MAXN;
   s.perm = reinterpret_cast<int*>(s.recip + MX_PANEL);
   s.cols = s.perm + MX_MAXN;
-  s.expA = s.cols + MX_MAXN;
-  s.expB = s.expA + MX_MAXN;
+  s.expA = s.cols + MX_MAXN;              // 2 MX_MAXN: the rows of a row-stacked product
+  s.expB = s.expA + 2 * MX_MAXN;
   s.red = reinterpret_cast<float*>(s.expB + MX_MAXN);
   s.mbar = reinterpret_cast<uint64_t*>(s.red + 32);
   s.tslot = reinterpret_cast<uint32_t*>(s.mbar + 2);
@@ -392,29 +392,32 @@ __device__ void oz_exponents(const double2* __restrict__ X, const double2* __res
   const int M = Xlo ? 2 * N : N;         // rows N.. of a row-stacked product come from Xlo
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   if (rows) {
-  for (int r = threadIdx.x; r < MX_MAXN; r += blockDim.x) s.expA[r] = 0;
+  for (int r = threadIdx.x; r < M; r += blockDim.x) s.expA[r] = 0;
   __syncthreads();
-  int rmax[MX_ROWS];
+  // rows in slabs of 32 MX_ROWS (a stacked product has up to 2 MX_MAXN)
+  for (int r0 = 0; r0 < M; r0 += 32 * MX_ROWS) {
+    int rmax[MX_ROWS];
 #pragma unroll
-  for (int m = 0; m < MX_ROWS; ++m) rmax[m] = 0;
-  // two columns of X per step so that twice the loads are in flight
-  for (int k = warp; k < N; k += 2 * nwarp) {
-    const size_t c0 = (size_t)k * N, c1 = (size_t)min(k + nwarp, N - 1) * N;
-    const bool two = k + nwarp < N;
+    for (int m = 0; m < MX_ROWS; ++m) rmax[m] = 0;
+    // two columns of X per step so that twice the loads are in flight
+    for (int k = warp; k < N; k += 2 * nwarp) {
+      const size_t c0 = (size_t)k * N, c1 = (size_t)min(k + nwarp, N - 1) * N;
+      const bool two = k + nwarp < N;
 #pragma unroll
-    for (int m = 0; m < MX_ROWS; ++m) {
-      const int i = lane + 32 * m;
-      if (i < M) {
-        const double2* xr = i < N ? X + i : Xlo + (i - N);
-        const double2 v0 = xr[c0];
-        const double2 v1 = two ? xr[c1] : v0;
-        rmax[m] = max(rmax[m], max(max(bexp(v0.x), bexp(v0.y)), max(bexp(v1.x), bexp(v1.y))));
+      for (int m = 0; m < MX_ROWS; ++m) {
+        const int i = r0 + lane + 32 * m;
+        if (i < M) {
+          const double2* xr = i < N ? X + i : Xlo + (i - N);
+          const double2 v0 = xr[c0];
+          const double2 v1 = two ? xr[c1] : v0;
+          rmax[m] = max(rmax[m], max(max(bexp(v0.x), bexp(v0.y)), max(bexp(v1.x), bexp(v1.y))));
+        }
       }
     }
-  }
 #pragma unroll
-  for (int m = 0; m < MX_ROWS; ++m)
-    if (lane + 32 * m < M) atomicMax(&s.expA[lane + 32 * m], rmax[m]);
+    for (int m = 0; m < MX_ROWS; ++m)
+      if (r0 + lane + 32 * m < M) atomicMax(&s.expA[r0 + lane + 32 * m], rmax[m]);
+  }
   }
   if (cols)
   for (int j = warp; j < N; j += 2 * nwarp) {
@@ -651,10 +654,11 @@ __device__ __forceinline__ double cabs64(double re, double im) {
 // bit 1: Y is the previous product's Y (column exponents in expB).
 constexpr int REUSE_X = 1, REUSE_Y = 2;
 
-// Rows N .. 2N-1 of a row-stacked product (2 Ndim <= 128): X' Y with its own
-// left factor, epilogue (EPI2 of oz_gemm) and outputs, in the same M = 128
-// tile as the first product's rows.  Each output element sees the same digits
-// and the same MMA sums as in a product of its own.
+// Rows N .. 2N-1 of a row-stacked product: X' Y with its own left factor,
+// epilogue (EPI2 of oz_gemm) and outputs, in the 128-row tiles that follow the
+// first product's rows (the first product's last, partly filled tile takes the
+// first rows of X').  Each output element sees the same digits and the same
+// MMA sums as in a product of its own.
 struct OzLower {
   const double2* X;
   double2* out0;
@@ -676,7 +680,8 @@ __device__ double oz_gemm(const double2* __restrict__ X, const double2* __restri
   double nrm_d = 0.0;
   oz_exponents(X, Y, N, s, !(reuse & REUSE_X), !(reuse & REUSE_Y), stacked ? lo.X : nullptr);
   __syncthreads();
-  for (int rb = 0; rb < pl.nrb && !st.abort; ++rb) {
+  const int nrb = stacked ? (M + 127) / 128 : pl.nrb;
+  for (int rb = 0; rb < nrb && !st.abort; ++rb) {
     const int rb0 = rb * 128;
     for (int pass = 0; pass < npass && !st.abort; ++pass) {
       const int cbi = pass;
@@ -1358,11 +1363,13 @@ __device__ __forceinline__ void mixed_solve(const MxPlan& pl, double2 w, const O
     if (mixed_inverse(E, w, pl, ns_iter, &G, &Gn, Mi, R, s, st, 1e-4f)) stat |= PT_SINGULAR;
     // the reference's six products (:92-116), ordered so that each shares an
     // operand with the one before it and reuses its exponents; eps still
-    // receives M1 beta before M2 alpha.  Up to Ndim 64 the products with a
-    // common right factor share one 128-row tile (rows of the second below
-    // those of the first): three products instead of six.
+    // receives M1 beta before M2 alpha.  Where it takes fewer 128-row tiles
+    // (Ndim mod 128 in 1..64: up to Ndim 64, or 129..192, 257..320), the
+    // products with a common right factor run as one product whose rows are
+    // those of the first and then those of the second: three products instead
+    // of six.
     double part;
-    if (2 * N <= 128) {
+    if ((2 * N + 127) / 128 < 2 * ((N + 127) / 128)) {
       oz_gemm<OZ_STORE, OZ_STORE>(Al, G, pl, M1, nullptr, nullptr, s, st, 0,
                                   OzLower{Be, M2, nullptr, nullptr});               // :92, :95
       oz_gemm<OZ_ADD2, OZ_STORE>(M1, Be, pl, E, ES, nullptr, s, st, 0,
@@ -1645,7 +1652,7 @@ size_t mixed_smem(int N, int wb = 0) {     // wb = 0: the built-in plan's width
   static_assert((MX_SMEM_GJ_N + 1) * MX_SMEM_GJ_N * 8 <= MX_FP64_AREA, "FP32 GJ area");
   static_assert(2 * MX_MAXN * MX_PANEL * 8 <= MX_FP64_AREA, "FP32 GJ panel area");
   const size_t planes = (size_t)planes_bytes_of(wb > 0 ? wb : pl.w0);
-  return planes + (size_t)MX_MAXN * 8 * 2 + MX_PANEL * 8 + (size_t)MX_MAXN * 4 * 4 + 32 * 4 +
+  return planes + (size_t)MX_MAXN * 8 * 2 + MX_PANEL * 8 + (size_t)MX_MAXN * 4 * 5 + 32 * 4 +
          16 + 8 + 16;
 }
 
